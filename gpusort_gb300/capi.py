@@ -1,0 +1,243 @@
+"""ctypes binding of the engine's C ABI (include/gpusort_gb300.h).
+
+The shared library is built in-tree (``gpusort_gb300/_lib``) by
+``gpusort_gb300._build``. Loading fails loudly when it is missing: there is
+no CPU fallback anywhere in the package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgpusort_gb300.so"
+
+# gs_status
+GS_OK = 0
+GS_ERR_EMPTY = 1
+GS_ERR_OOM = 2
+GS_ERR_BAD_DTYPE = 3
+GS_ERR_TIMEOUT = 4
+GS_ERR_CUDA = 5
+GS_ERR_INVALID = 6
+GS_ERR_NO_DEVICE = 7
+GS_ERR_TOO_LARGE = 8
+GS_ERR_BUSY = 9
+
+# gs_dtype
+GS_U32, GS_I32, GS_F32, GS_U64, GS_I64, GS_F64 = range(6)
+
+FLAG_DESCENDING = 0x1
+FLAG_PAIRS_STABLE = 0x2
+FLAG_HOST = 0x4
+FLAG_SYNC = 0x8
+
+ALGO_AUTO, ALGO_RADIX, ALGO_SAMPLE, ALGO_HYK = range(4)
+
+DEBUG_SPIN_LIMIT = 1
+DEBUG_INJECT_STALL = 2
+DEBUG_BUDGET = 3
+
+# Every symbol include/gpusort_gb300.h declares (checked by the CPU tests).
+EXPORTED = [
+    "gs_version", "gs_device_count", "gs_ctx_create", "gs_ctx_destroy",
+    "gs_ctx_set_stream", "gs_ctx_synchronize", "gs_last_error",
+    "gs_last_global_error", "gs_sort_keys", "gs_sort_pairs",
+    "gs_segmented_sort_keys", "gs_gather", "gs_phase_times",
+    "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set",
+]
+
+_NP_DTYPE = {
+    np.dtype(np.uint32): GS_U32, np.dtype(np.int32): GS_I32, np.dtype(np.float32): GS_F32,
+    np.dtype(np.uint64): GS_U64, np.dtype(np.int64): GS_I64, np.dtype(np.float64): GS_F64,
+}
+
+
+class gs_opts(C.Structure):
+    _fields_ = [("algo", C.c_uint32), ("partitions", C.c_uint32), ("k_way", C.c_uint32),
+                ("oversample", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class GsError(RuntimeError):
+    """A non-OK gs_status, with the engine's message."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"gs_status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load() -> C.CDLL:
+    """Load the engine library (built in-tree). Raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not _LIB_PATH.exists():
+            raise RuntimeError(
+                f"gpusort_gb300 native library not built: {_LIB_PATH} is missing "
+                "(run gpusort_gb300._build.build())")
+        L = C.CDLL(str(_LIB_PATH))
+        vp, u64, u32, i32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int
+        L.gs_version.restype = u32
+        L.gs_device_count.restype = i32
+        L.gs_ctx_create.argtypes = [i32, u64]
+        L.gs_ctx_create.restype = vp
+        L.gs_ctx_destroy.argtypes = [vp]
+        L.gs_ctx_destroy.restype = None
+        L.gs_ctx_set_stream.argtypes = [vp, vp]
+        L.gs_ctx_synchronize.argtypes = [vp]
+        L.gs_last_error.argtypes = [vp]
+        L.gs_last_error.restype = C.c_char_p
+        L.gs_last_global_error.restype = C.c_char_p
+        L.gs_sort_keys.argtypes = [vp, i32, vp, vp, u64, u32, C.POINTER(gs_opts)]
+        L.gs_sort_pairs.argtypes = [vp, i32, i32, vp, vp, vp, vp, u64, u32, C.POINTER(gs_opts)]
+        L.gs_segmented_sort_keys.argtypes = [vp, i32, vp, vp, u64, vp, u32, u32]
+        L.gs_gather.argtypes = [vp, vp, vp, u64, u32, vp, u32]
+        L.gs_phase_times.argtypes = [vp, C.POINTER(C.c_char_p), C.POINTER(C.c_double), i32]
+        L.gs_phase_times.restype = i32
+        L.gs_ctx_set_timing.argtypes = [vp, i32]
+        L.gs_kernel_times.argtypes = [vp, C.POINTER(C.c_double), i32]
+        L.gs_kernel_times.restype = i32
+        L.gs_debug_set.argtypes = [vp, i32, u64]
+        for fn in ("gs_ctx_set_stream", "gs_ctx_synchronize", "gs_sort_keys", "gs_sort_pairs",
+                   "gs_segmented_sort_keys", "gs_gather", "gs_ctx_set_timing", "gs_debug_set"):
+            getattr(L, fn).restype = i32
+        _lib = L
+        return L
+
+
+def dtype_code(dt) -> int:
+    """gs_dtype of a numpy or torch dtype."""
+    try:
+        import torch
+        tmap = {torch.int32: GS_I32, torch.float32: GS_F32, torch.int64: GS_I64,
+                torch.float64: GS_F64}
+        for name, code in (("uint32", GS_U32), ("uint64", GS_U64)):
+            if hasattr(torch, name):
+                tmap[getattr(torch, name)] = code
+        if dt in tmap:
+            return tmap[dt]
+    except ImportError:
+        pass
+    d = np.dtype(dt)
+    if d not in _NP_DTYPE:
+        raise GsError(GS_ERR_BAD_DTYPE, f"unsupported dtype {dt}")
+    return _NP_DTYPE[d]
+
+
+def _count(x) -> int:
+    return int(x.numel()) if hasattr(x, "numel") else int(x.size)
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+class Context:
+    """One engine context (device, stream, scratch within an HBM budget)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.L = load()
+        h = self.L.gs_ctx_create(device, hbm_budget_bytes)
+        if not h:
+            raise GsError(GS_ERR_NO_DEVICE, self.L.gs_last_global_error().decode())
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != GS_OK:
+            raise GsError(st, self.L.gs_last_error(self.h).decode())
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.L.gs_ctx_set_stream(self.h, stream_handle or None))
+
+    def synchronize(self):
+        self._check(self.L.gs_ctx_synchronize(self.h))
+
+    def status_synchronize(self) -> int:
+        return self.L.gs_ctx_synchronize(self.h)
+
+    def last_error(self) -> str:
+        return self.L.gs_last_error(self.h).decode()
+
+    @staticmethod
+    def _opts(algo=ALGO_AUTO, partitions=0, k_way=0, oversample=0, seed=0):
+        return gs_opts(algo, partitions, k_way, oversample, seed)
+
+    def sort_keys(self, keys_in, keys_out, *, descending=False, flags=0, n=None, dtype=None,
+                  algo=ALGO_AUTO, partitions=0, k_way=0, oversample=0, seed=0) -> int:
+        """Sort device tensors (or host arrays with FLAG_HOST). `dtype` (a numpy
+        dtype) overrides the element type, e.g. to sort int32-typed torch
+        storage as uint32. Returns gs_status."""
+        n = _count(keys_in) if n is None else int(n)
+        f = flags | (FLAG_DESCENDING if descending else 0)
+        o = self._opts(algo, partitions, k_way, oversample, seed)
+        code = dtype_code(dtype if dtype is not None else keys_in.dtype)
+        return self.L.gs_sort_keys(self.h, code, _ptr(keys_in), _ptr(keys_out), n, f, C.byref(o))
+
+    def sort_pairs(self, keys_in, vals_in, keys_out, vals_out, *, descending=False,
+                   stable=False, flags=0, n=None, key_dtype=None, val_dtype=None,
+                   algo=ALGO_AUTO, partitions=0, k_way=0, oversample=0, seed=0) -> int:
+        n = _count(keys_in) if n is None else int(n)
+        f = flags | (FLAG_DESCENDING if descending else 0) | (FLAG_PAIRS_STABLE if stable else 0)
+        o = self._opts(algo, partitions, k_way, oversample, seed)
+        kc = dtype_code(key_dtype if key_dtype is not None else keys_in.dtype)
+        vc = dtype_code(val_dtype if val_dtype is not None else vals_in.dtype)
+        return self.L.gs_sort_pairs(self.h, kc, vc, _ptr(keys_in), _ptr(vals_in), _ptr(keys_out),
+                                    _ptr(vals_out), n, f, C.byref(o))
+
+    def segmented_sort_keys(self, keys_in, keys_out, offsets, nseg, *, descending=False,
+                            flags=0, n=None, dtype=None) -> int:
+        n = _count(keys_in) if n is None else int(n)
+        f = flags | (FLAG_DESCENDING if descending else 0)
+        code = dtype_code(dtype if dtype is not None else keys_in.dtype)
+        return self.L.gs_segmented_sort_keys(self.h, code, _ptr(keys_in), _ptr(keys_out), n,
+                                             _ptr(offsets), nseg, f)
+
+    def gather(self, src, dst, perm, elem_bytes, flags=0) -> int:
+        n = _count(perm)
+        return self.L.gs_gather(self.h, _ptr(src), _ptr(dst), n, elem_bytes, _ptr(perm), flags)
+
+    def set_timing(self, enable: bool):
+        self._check(self.L.gs_ctx_set_timing(self.h, int(enable)))
+
+    def phase_times(self) -> dict:
+        names = (C.c_char_p * 8)()
+        ms = (C.c_double * 8)()
+        k = self.L.gs_phase_times(self.h, names, ms, 8)
+        return {names[i].decode(): ms[i] for i in range(min(k, 8))}
+
+    def kernel_times(self) -> list[float]:
+        """[upsweep, plan, pass 0, pass 1, ...] device ms of the last sort."""
+        ms = (C.c_double * 32)()
+        k = self.L.gs_kernel_times(self.h, ms, 32)
+        return [ms[i] for i in range(min(k, 32))]
+
+    def debug_set(self, key: int, value: int):
+        self._check(self.L.gs_debug_set(self.h, key, value))

@@ -1,0 +1,440 @@
+// C ABI of the engine (include/gpusort_gb300.h): contexts, scratch held
+// within an HBM budget, host staging, dispatch to the kernel launchers.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gpusort_gb300.h"
+#include "engine.h"
+#include "common.cuh"
+
+namespace {
+
+thread_local std::string g_last_global_error;
+
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gs_ctx {
+  gs::DeviceProps props;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  uint64_t budget = 0;  // 0: no cap
+  uint64_t held = 0;
+  uint32_t gen = 0;
+  uint32_t spin_limit = 1u << 20;
+  uint32_t inject_stall = 0;
+  bool timing = false;
+  gs::SortWork* work = nullptr;
+  uint32_t* err = nullptr;
+  DevBuf status;     // look-back words
+  DevBuf alt_k, alt_v;
+  DevBuf stage_k, stage_v, stage_off;
+  // phase timing
+  cudaEvent_t ev[8] = {};
+  int n_phases = 0;
+  const char* phase_names[8] = {};
+  double phase_ms[8] = {};
+  // kernel timing of the last radix pipeline (3 + MAX_DIGITS marks)
+  cudaEvent_t kev[3 + 16] = {};
+  int n_kev = 0;
+  uint32_t kev_exec_mask = 0;
+};
+
+namespace {
+
+gs_status fail(gs_ctx* ctx, gs_status st, const std::string& msg) {
+  if (ctx) ctx->last_error = msg; else g_last_global_error = msg;
+  return st;
+}
+
+gs_status cuda_fail(gs_ctx* ctx, cudaError_t e, const char* where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(ctx, GS_ERR_OOM, m);
+  return fail(ctx, GS_ERR_CUDA, m);
+}
+
+// Grow-only scratch, bounded by the context's HBM budget.
+gs_status ensure(gs_ctx* ctx, DevBuf& b, size_t bytes, bool zero = false) {
+  if (b.bytes >= bytes) return GS_OK;
+  size_t want = bytes;
+  const uint64_t next_held = ctx->held - b.bytes + want;
+  if (ctx->budget && next_held > ctx->budget) {
+    return fail(ctx, GS_ERR_OOM, "HBM budget exceeded: need " + std::to_string(next_held) +
+                                     " bytes, budget " + std::to_string(ctx->budget));
+  }
+  if (b.ptr) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(b.ptr);
+    ctx->held -= b.bytes;
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.ptr, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.ptr = nullptr;
+    return fail(ctx, GS_ERR_OOM, "cudaMalloc of " + std::to_string(want) + " bytes failed");
+  }
+  if (zero) {
+    e = cudaMemsetAsync(b.ptr, 0, want, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync");
+  }
+  b.bytes = want;
+  ctx->held += want;
+  return GS_OK;
+}
+
+bool dtype_info(gs_dtype t, int* bytes, uint32_t* kind) {
+  switch (t) {
+    case GS_U32: *bytes = 4; *kind = gs::KIND_UNSIGNED; return true;
+    case GS_I32: *bytes = 4; *kind = gs::KIND_SIGNED; return true;
+    case GS_F32: *bytes = 4; *kind = gs::KIND_FLOAT; return true;
+    case GS_U64: *bytes = 8; *kind = gs::KIND_UNSIGNED; return true;
+    case GS_I64: *bytes = 8; *kind = gs::KIND_SIGNED; return true;
+    case GS_F64: *bytes = 8; *kind = gs::KIND_FLOAT; return true;
+  }
+  return false;
+}
+
+constexpr uint64_t MAX_N = 0xFFFFFFFFull;  // 32-bit bin counters
+
+void phase_reset(gs_ctx* ctx) { ctx->n_phases = 0; }
+
+void phase_mark(gs_ctx* ctx, const char* name) {
+  if (!ctx->timing || ctx->n_phases >= 7) return;
+  if (ctx->n_phases == 0) cudaEventRecord(ctx->ev[0], ctx->stream);
+  ctx->phase_names[ctx->n_phases] = name;
+  ctx->n_phases++;
+  cudaEventRecord(ctx->ev[ctx->n_phases], ctx->stream);
+}
+
+// Bring the look-back status words to the size a job needs and keep the
+// generation tags unambiguous.
+gs_status prepare_status(gs_ctx* ctx, size_t words, uint32_t passes) {
+  gs_status st = ensure(ctx, ctx->status, words * sizeof(uint64_t), true);
+  if (st != GS_OK) return st;
+  if (ctx->gen + passes + 1 >= gs::GEN_MASK) {
+    cudaError_t e = cudaMemsetAsync(ctx->status.ptr, 0, ctx->status.bytes, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(status)");
+    ctx->gen = 0;
+  }
+  return GS_OK;
+}
+
+gs_status check_err_word(gs_ctx* ctx) {
+  uint32_t h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, ctx->err, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                  ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+  if (h) {
+    cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    std::string m = "device wait ran out or scatter out of range (code " + std::to_string(h) + ")";
+    return fail(ctx, GS_ERR_TIMEOUT, m);
+  }
+  if (ctx->timing && ctx->n_phases > 0) {
+    for (int i = 0; i < ctx->n_phases; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+      ctx->phase_ms[i] = ms;
+    }
+  }
+  return GS_OK;
+}
+
+// Device-memory radix sort of keys or pairs.
+gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind,
+                      const void* kin, const void* vin, void* kout, void* vout,
+                      uint64_t n, uint32_t flags) {
+  const bool desc = flags & GS_FLAG_DESCENDING;
+  const bool stable = flags & GS_FLAG_PAIRS_STABLE;
+  gs::RadixJob job;
+  job.keys_in = kin;
+  job.keys_out = kout;
+  job.vals_in = vin;
+  job.vals_out = vout;
+  job.n = n;
+  job.key_bytes = kb;
+  job.val_bytes = vb;
+  job.key_kind = kkind;
+  job.val_kind = vkind;
+  job.desc = desc;
+  job.ties_by_value = vb > 0 && !stable;
+  job.reverse_first = vb > 0 && stable && desc;
+  job.work = ctx->work;
+  job.err = ctx->err;
+  job.spin_limit = ctx->spin_limit;
+  job.inject_stall = ctx->inject_stall;
+  ctx->inject_stall = 0;
+
+  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st != GS_OK) return st;
+  job.keys_alt = ctx->alt_k.ptr;
+  if (vb) {
+    st = ensure(ctx, ctx->alt_v, size_t(n) * vb);
+    if (st != GS_OK) return st;
+    job.vals_alt = ctx->alt_v.ptr;
+  }
+  const uint32_t passes = uint32_t(kb + (job.ties_by_value ? vb : 0));
+  st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), passes);
+  if (st != GS_OK) return st;
+  job.status = static_cast<uint64_t*>(ctx->status.ptr);
+  if (ctx->timing) {
+    job.marks = ctx->kev;
+    ctx->n_kev = 3 + int(kb + (job.ties_by_value ? vb : 0));
+  }
+  cudaError_t e = gs::launch_radix_sort(job, ctx->props, &ctx->gen, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "radix sort launch");
+  return GS_OK;
+}
+
+gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const void* kin,
+                      const void* vin, void* kout, void* vout, uint64_t n, uint32_t flags,
+                      const gs_opts* opts) {
+  (void)opts;
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int kb = 0, vb = 0;
+  uint32_t kk = 0, vk = 0;
+  if (!dtype_info(kt, &kb, &kk)) return fail(ctx, GS_ERR_BAD_DTYPE, "unknown key dtype");
+  if (has_v && !dtype_info(vt, &vb, &vk)) return fail(ctx, GS_ERR_BAD_DTYPE, "unknown value dtype");
+  if (n == 0) return fail(ctx, GS_ERR_EMPTY, "No data to sort.");
+  if (n > MAX_N) return fail(ctx, GS_ERR_TOO_LARGE, "n exceeds 2^32-1 elements");
+  if (!kin || !kout || (has_v && (!vin || !vout)))
+    return fail(ctx, GS_ERR_INVALID, "null data pointer");
+  cudaError_t e = cudaSetDevice(ctx->props.device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  phase_reset(ctx);
+
+  if (flags & GS_FLAG_HOST) {
+    gs_status st = ensure(ctx, ctx->stage_k, size_t(n) * kb);
+    if (st != GS_OK) return st;
+    if (has_v) {
+      st = ensure(ctx, ctx->stage_v, size_t(n) * vb);
+      if (st != GS_OK) return st;
+    }
+    if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
+    e = cudaMemcpyAsync(ctx->stage_k.ptr, kin, size_t(n) * kb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && has_v)
+      e = cudaMemcpyAsync(ctx->stage_v.ptr, vin, size_t(n) * vb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "host to device copy");
+    if (ctx->timing) { ctx->n_phases = 0; phase_mark(ctx, "Transfer in"); }
+    st = device_sort(ctx, kb, kk, vb, vk, ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr,
+                     ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr, n, flags);
+    if (st != GS_OK) return st;
+    phase_mark(ctx, "Local sort");
+    e = cudaMemcpyAsync(kout, ctx->stage_k.ptr, size_t(n) * kb, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && has_v)
+      e = cudaMemcpyAsync(vout, ctx->stage_v.ptr, size_t(n) * vb, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device to host copy");
+    phase_mark(ctx, "Transfer out");
+    return check_err_word(ctx);
+  }
+
+  if (ctx->timing) { cudaEventRecord(ctx->ev[0], ctx->stream); }
+  gs_status st = device_sort(ctx, kb, kk, vb, vk, kin, has_v ? vin : nullptr, kout,
+                             has_v ? vout : nullptr, n, flags);
+  if (st != GS_OK) return st;
+  phase_mark(ctx, "Local sort");
+  if (flags & GS_FLAG_SYNC) return check_err_word(ctx);
+  return GS_OK;
+}
+
+__global__ void gather_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                              uint64_t n, uint32_t eb, const uint64_t* __restrict__ perm) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t s = perm[i];
+    if (s >= n) continue;
+    if (eb == 4) {
+      reinterpret_cast<uint32_t*>(out)[i] = reinterpret_cast<const uint32_t*>(in)[s];
+    } else if (eb == 8) {
+      reinterpret_cast<uint64_t*>(out)[i] = reinterpret_cast<const uint64_t*>(in)[s];
+    } else {
+      for (uint32_t b = 0; b < eb; ++b) out[i * eb + b] = in[s * eb + b];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t gs_version(void) { return 0x000100u; }
+
+int gs_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+const char* gs_last_global_error(void) { return g_last_global_error.c_str(); }
+
+const char* gs_last_error(gs_ctx* ctx) {
+  if (!ctx) return g_last_global_error.c_str();
+  return ctx->last_error.c_str();
+}
+
+gs_ctx* gs_ctx_create(int device, uint64_t hbm_budget_bytes) {
+  int ndev = gs_device_count();
+  if (ndev == 0) {
+    g_last_global_error = "No CUDA-capable devices were detected";
+    return nullptr;
+  }
+  if (device < 0 || device >= ndev) {
+    g_last_global_error = "invalid device ordinal";
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    g_last_global_error = "cudaSetDevice failed";
+    return nullptr;
+  }
+  gs_ctx* ctx = new gs_ctx();
+  ctx->props.device = device;
+  cudaDeviceGetAttribute(&ctx->props.num_sms, cudaDevAttrMultiProcessorCount, device);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  ctx->props.smem_optin = size_t(optin);
+  ctx->budget = hbm_budget_bytes;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_last_global_error = "cudaStreamCreate failed";
+    delete ctx;
+    return nullptr;
+  }
+  ctx->stream = ctx->own_stream;
+  if (cudaMalloc(&ctx->work, gs::sort_work_bytes()) != cudaSuccess ||
+      cudaMalloc(&ctx->err, 256) != cudaSuccess) {
+    g_last_global_error = "cudaMalloc of the context's work area failed";
+    cudaGetLastError();
+    gs_ctx_destroy(ctx);
+    return nullptr;
+  }
+  ctx->held += gs::sort_work_bytes() + 256;
+  cudaMemsetAsync(ctx->err, 0, 256, ctx->stream);
+  for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  for (auto& ev : ctx->kev) cudaEventCreate(&ev);
+  cudaStreamSynchronize(ctx->stream);
+  return ctx;
+}
+
+void gs_ctx_destroy(gs_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->props.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  DevBuf* bufs[] = {&ctx->status, &ctx->alt_k, &ctx->alt_v, &ctx->stage_k, &ctx->stage_v,
+                    &ctx->stage_off};
+  for (DevBuf* b : bufs) if (b->ptr) cudaFree(b->ptr);
+  if (ctx->work) cudaFree(ctx->work);
+  if (ctx->err) cudaFree(ctx->err);
+  for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+  for (auto& ev : ctx->kev) if (ev) cudaEventDestroy(ev);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+gs_status gs_ctx_set_stream(gs_ctx* ctx, void* stream) {
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->stream = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
+  return GS_OK;
+}
+
+gs_status gs_ctx_synchronize(gs_ctx* ctx) {
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->props.device);
+  return check_err_word(ctx);
+}
+
+gs_status gs_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in, void* out, uint64_t n,
+                       uint32_t flags, const gs_opts* opts) {
+  return sort_common(ctx, dtype, 0, GS_U32, in, nullptr, out, nullptr, n, flags, opts);
+}
+
+gs_status gs_sort_pairs(gs_ctx* ctx, gs_dtype key_dtype, gs_dtype val_dtype, const void* keys_in,
+                        const void* vals_in, void* keys_out, void* vals_out, uint64_t n,
+                        uint32_t flags, const gs_opts* opts) {
+  return sort_common(ctx, key_dtype, 1, val_dtype, keys_in, vals_in, keys_out, vals_out, n, flags,
+                     opts);
+}
+
+gs_status gs_segmented_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in, void* out,
+                                 uint64_t n, const uint64_t* offsets, uint32_t nseg,
+                                 uint32_t flags) {
+  (void)dtype; (void)in; (void)out; (void)n; (void)offsets; (void)nseg; (void)flags;
+  return fail(ctx, GS_ERR_INVALID, "segmented sort is not available in this build");
+}
+
+gs_status gs_gather(gs_ctx* ctx, const void* in, void* out, uint64_t n, uint32_t elem_bytes,
+                    const uint64_t* perm, uint32_t flags) {
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (n == 0) return GS_OK;
+  if (!in || !out || !perm || elem_bytes == 0 || elem_bytes > 64)
+    return fail(ctx, GS_ERR_INVALID, "bad gather arguments");
+  if (flags & GS_FLAG_HOST) return fail(ctx, GS_ERR_INVALID, "gather takes device pointers");
+  cudaSetDevice(ctx->props.device);
+  unsigned blocks = unsigned((n + 255) / 256);
+  const unsigned cap = unsigned(ctx->props.num_sms) * 8;
+  if (blocks > cap) blocks = cap;
+  gather_kernel<<<blocks, 256, 0, ctx->stream>>>(static_cast<const uint8_t*>(in),
+                                                 static_cast<uint8_t*>(out), n, elem_bytes, perm);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gather launch");
+  if (flags & GS_FLAG_SYNC) return check_err_word(ctx);
+  return GS_OK;
+}
+
+int gs_kernel_times(gs_ctx* ctx, double* ms, int cap) {
+  if (!ctx || !ctx->timing || ctx->n_kev < 3) return 0;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaEventSynchronize(ctx->kev[ctx->n_kev - 1]);
+  int k = 0;
+  for (int i = 1; i < ctx->n_kev && k < cap; ++i, ++k) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ctx->kev[i - 1], ctx->kev[i]);
+    ms[k] = t;
+  }
+  return ctx->n_kev - 1;
+}
+
+int gs_phase_times(gs_ctx* ctx, const char** names, double* ms, int cap) {
+  if (!ctx) return 0;
+  int n = ctx->n_phases;
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (names) names[i] = ctx->phase_names[i];
+    if (ms) ms[i] = ctx->phase_ms[i];
+  }
+  return n;
+}
+
+gs_status gs_ctx_set_timing(gs_ctx* ctx, int enable) {
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  ctx->timing = enable != 0;
+  return GS_OK;
+}
+
+gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value) {
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  switch (key) {
+    case GS_DEBUG_SPIN_LIMIT: ctx->spin_limit = value ? uint32_t(value) : 1u; return GS_OK;
+    case GS_DEBUG_INJECT_STALL: ctx->inject_stall = value ? 1u : 0u; return GS_OK;
+    case GS_DEBUG_BUDGET: ctx->budget = value; return GS_OK;
+  }
+  return fail(ctx, GS_ERR_INVALID, "unknown debug key");
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+// Host-side internal interfaces between the C ABI (capi.cu) and the kernel
+// launchers (radix.cu, ...). Not installed; include/gpusort_gb300.h is the
+// public surface.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gs {
+
+struct SortWork;
+
+struct DeviceProps {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+};
+
+// One radix sort of keys (and an optional payload) on device memory.
+struct RadixJob {
+  const void* keys_in = nullptr;
+  void* keys_out = nullptr;
+  void* keys_alt = nullptr;         // n * key_bytes scratch
+  const void* vals_in = nullptr;
+  void* vals_out = nullptr;
+  void* vals_alt = nullptr;         // n * val_bytes scratch
+  uint64_t n = 0;
+  int key_bytes = 4;                // 4 or 8
+  int val_bytes = 0;                // 0 (keys only), 4 or 8
+  uint32_t key_kind = 0, val_kind = 0;
+  bool desc = false;
+  bool ties_by_value = false;       // value digits take part in the order
+  bool reverse_first = false;       // stable descending pairs
+  uint64_t* status = nullptr;       // radix_status_words(n, ...) words
+  SortWork* work = nullptr;
+  uint32_t* err = nullptr;
+  uint32_t spin_limit = 1u << 20;
+  uint32_t inject_stall = 0;
+  // Optional timing marks: when set, an event is recorded before the
+  // pipeline (marks[0]), after the upsweep (1), after the plan (2) and after
+  // each pass q (3 + q). Needs 3 + digits events.
+  cudaEvent_t* marks = nullptr;
+};
+
+// Tile size (elements) of the pass kernel for a key/value width pair.
+uint32_t radix_tile(int key_bytes, int val_bytes);
+// Look-back words a job of n elements needs.
+size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
+size_t sort_work_bytes();
+
+// Enqueue the whole radix pipeline on `stream`. `gen` is the context's
+// launch-generation counter (advanced once per pass launch); the caller
+// clears the status words when it wraps.
+cudaError_t launch_radix_sort(const RadixJob& job, const DeviceProps& props,
+                              uint32_t* gen, cudaStream_t stream);
+
+}  // namespace gs

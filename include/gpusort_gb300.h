@@ -1,0 +1,197 @@
+/*
+ * gpusort_gb300.h - C ABI of the GB300 sorting engine.
+ *
+ * Plain C: pointers, sizes and status codes only. Every entry point below
+ * replaces one reference interface on the sort path of monotone-RK/gpusort;
+ * the citation beside it names that interface (path:line in the reference
+ * project). The header-only C++ layer in include/gpusort/ keeps the
+ * reference's templated names (HykSort, SampleSort, HyperQuickSort) and
+ * calls these functions.
+ *
+ * Memory: by default every pointer is a device pointer on the context's
+ * device and the call is asynchronous on the context's stream. With
+ * GS_FLAG_HOST every pointer is host memory and the call is synchronous
+ * (copy in, sort, copy out), which is how the reference's own API behaves
+ * (src/cuda_utils.cu:403-445 stages host data through the device).
+ */
+#ifndef GPUSORT_GB300_H_
+#define GPUSORT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference raises C++ exceptions instead
+ * (include/exceptions/thrust_exception.h:9-22,
+ *  include/exceptions/mpi_exception.h:9-22); the C++ layer maps these
+ * back to the same exception types and messages. */
+typedef enum gs_status {
+  GS_OK = 0,
+  GS_ERR_EMPTY = 1,        /* n == 0: "No data to sort."
+                              (include/helpers/hyksort_helper.h:105) */
+  GS_ERR_OOM = 2,          /* device allocation or HBM budget exhausted
+                              (src/cuda_utils.cu:415-416,425-426) */
+  GS_ERR_BAD_DTYPE = 3,    /* key/value type outside the instantiated set
+                              (src/cuda_utils.cu:257-318) */
+  GS_ERR_TIMEOUT = 4,      /* a bounded inter-block wait ran out; the
+                              result is invalid, the context stays usable */
+  GS_ERR_CUDA = 5,         /* CUDA runtime error (src/cuda_utils.cu:373-393) */
+  GS_ERR_INVALID = 6,      /* bad argument (null pointer, bad option) */
+  GS_ERR_NO_DEVICE = 7,    /* no CUDA device (src/cuda_utils.cu:81-92) */
+  GS_ERR_TOO_LARGE = 8,    /* n beyond the engine's per-call limit */
+  GS_ERR_BUSY = 9          /* serving queue full / request not finished */
+} gs_status;
+
+/* Key and value element types: the reference's instantiation set
+ * (src/cuda_utils.cu:257-262): int, unsigned int, float, double, int64_t,
+ * uint64_t. */
+typedef enum gs_dtype {
+  GS_U32 = 0,
+  GS_I32 = 1,
+  GS_F32 = 2,
+  GS_U64 = 3,
+  GS_I64 = 4,
+  GS_F64 = 5
+} gs_dtype;
+
+/* Flags (bitwise OR). */
+#define GS_FLAG_DESCENDING   0x1u  /* std::greater<T> instead of std::less<T>
+                                      (include/common.h:156-164,205-213) */
+#define GS_FLAG_PAIRS_STABLE 0x2u  /* pairs: ties on the key keep input order
+                                      (ascending) or reverse input order
+                                      (descending); equals the reference's
+                                      (key, value) order when values grow
+                                      along the input, e.g. global indexes
+                                      (include/hyksort_common_vector.inl:
+                                      552-565). Without it, ties are ordered by
+                                      value like std::pair's operator<
+                                      (include/helpers/hyksort_helper.h:
+                                      266-280). */
+#define GS_FLAG_HOST         0x4u  /* pointers are host memory; synchronous */
+#define GS_FLAG_SYNC         0x8u  /* wait for completion and report
+                                      GS_ERR_TIMEOUT from this call */
+
+/* Sorting strategy. Every strategy produces the same bytes. */
+typedef enum gs_algo {
+  GS_ALGO_AUTO = 0,       /* engine's fastest path for the size and type */
+  GS_ALGO_RADIX = 1,      /* one onesweep LSD radix sort over the array */
+  GS_ALGO_SAMPLE = 2,     /* SampleSort shape: splitters from an oversampled
+                             sample, bucket scatter into p partitions (the
+                             in-HBM Alltoallv), radix sort per partition
+                             (include/helpers/samplesort_helper.h:390-565) */
+  GS_ALGO_HYK = 3         /* HykSort shape: radix sort of p input partitions,
+                             k-way splitters, merge-path merge of the
+                             received runs
+                             (include/helpers/hyksort_helper.h:307-633) */
+} gs_algo;
+
+typedef struct gs_opts {
+  uint32_t algo;          /* gs_algo */
+  uint32_t partitions;    /* p: virtual MPI ranks (0 = engine default) */
+  uint32_t k_way;         /* HykSort k (0 = 4) */
+  uint32_t oversample;    /* samples per partition (0 = 32) */
+  uint64_t seed;          /* splitter sampling seed */
+} gs_opts;
+
+typedef struct gs_ctx gs_ctx;
+
+/* Library version, e.g. 0x000100 for 0.1.0. */
+uint32_t gs_version(void);
+
+/* Number of visible CUDA devices (src/cuda_utils.cu:81-92
+ * CudaUtils::GetDeviceCount). Returns 0 when there is none. */
+int gs_device_count(void);
+
+/* Create a context bound to `device`. `hbm_budget_bytes` caps the scratch
+ * the context may hold (0 = no cap). Replaces the per-call device selection
+ * and chunking of src/cuda_utils.cu:395-401,508-520: data stays resident
+ * and no chunk split is needed while it fits. Returns NULL on failure
+ * (gs_last_global_error() says why). */
+gs_ctx* gs_ctx_create(int device, uint64_t hbm_budget_bytes);
+void gs_ctx_destroy(gs_ctx* ctx);
+
+/* Use an existing CUDA stream (cudaStream_t passed as void*) for all later
+ * work of the context; NULL selects the CUDA legacy default stream. A new
+ * context uses a non-blocking stream of its own. */
+gs_status gs_ctx_set_stream(gs_ctx* ctx, void* stream);
+
+/* Wait for all work of the context. Returns GS_ERR_TIMEOUT if a bounded
+ * wait inside a kernel ran out since the last check (and clears it). */
+gs_status gs_ctx_synchronize(gs_ctx* ctx);
+
+/* Text of the last error on this context. */
+const char* gs_last_error(gs_ctx* ctx);
+const char* gs_last_global_error(void);
+
+/* Sort keys.
+ * Replaces CudaUtils::Sort (src/cuda_utils.cu:97-167) as called from
+ * HykSortHelper::Sort (include/helpers/hyksort_helper.h:94-145) and the
+ * whole SortAmongProcesses exchange (include/helpers/hyksort_helper.h:
+ * 453-536; include/helpers/samplesort_helper.h:420-501): the output is the
+ * concatenation of all ranks' slices, i.e. the globally sorted array.
+ * `in` and `out` may alias (in-place). */
+gs_status gs_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in, void* out,
+                       uint64_t n, uint32_t flags, const gs_opts* opts);
+
+/* Sort key/value pairs.
+ * Replaces CudaUtils::SortByKey (src/cuda_utils.cu:169-243) and
+ * HykSortHelper::SortByKey (include/helpers/hyksort_helper.h:224-297).
+ * Ties on the key are ordered by value (std::pair order) unless
+ * GS_FLAG_PAIRS_STABLE is set. Outputs may alias inputs. */
+gs_status gs_sort_pairs(gs_ctx* ctx, gs_dtype key_dtype, gs_dtype val_dtype,
+                        const void* keys_in, const void* vals_in,
+                        void* keys_out, void* vals_out, uint64_t n,
+                        uint32_t flags, const gs_opts* opts);
+
+/* Sort many independent segments in one call. Segment s is
+ * [offsets[s], offsets[s+1]) of `in`; `offsets` has nseg+1 entries and is a
+ * device pointer (host pointer with GS_FLAG_HOST), non-decreasing, with
+ * offsets[0] == 0. Each segment is sorted on its own, as if it were one
+ * rank's local sort (include/omp/omp_utils.h:147-207 applied per segment).
+ * Empty segments are allowed. */
+gs_status gs_segmented_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in,
+                                 void* out, uint64_t n, const uint64_t* offsets,
+                                 uint32_t nseg, uint32_t flags);
+
+/* Apply a permutation to a value array: out[i] = in[perm[i]], element size
+ * `elem_bytes` (1..64 bytes). Replaces ParUtils::ArrangeValues
+ * (include/par/par_utils.h:23-86), which moves each value vector to where
+ * its key went after a sort of (key, global index). */
+gs_status gs_gather(gs_ctx* ctx, const void* in, void* out, uint64_t n,
+                    uint32_t elem_bytes, const uint64_t* perm, uint32_t flags);
+
+/* Per-phase device times (milliseconds) of the last completed sort on this
+ * context, named like the reference's benchmark timers
+ * (include/helpers/hyksort_helper.h:643-650): "Local sort",
+ * "Select splitters", "Exchange data", "Merge data", "Total". Writes up to
+ * `cap` (name, ms) entries; returns how many exist. Names are static
+ * strings. Only filled when timing was enabled with gs_ctx_set_timing. */
+int gs_phase_times(gs_ctx* ctx, const char** names, double* ms, int cap);
+gs_status gs_ctx_set_timing(gs_ctx* ctx, int enable);
+
+/* Device time (ms) of each kernel of the last radix pipeline when timing is
+ * on: [0] upsweep histogram (with its memset), [1] plan, [2 + q] pass of
+ * digit q (about 0 when the digit was skipped). Returns the entry count.
+ * The reference's GPU sub-phase timers ("Local sort sort/transfer/merge",
+ * src/cuda_utils.cu:29-34) are the counterpart. */
+int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
+
+/* Test hooks for failure detection without a GPU fault.
+ * GS_DEBUG_SPIN_LIMIT: iteration cap of every inter-block wait.
+ * GS_DEBUG_INJECT_STALL: when non-zero, one tile of the next sort waits for
+ * a predecessor flag that is never set, so the wait runs out after the spin
+ * limit and the call reports GS_ERR_TIMEOUT.
+ * GS_DEBUG_BUDGET: replace the HBM budget (bytes). */
+#define GS_DEBUG_SPIN_LIMIT   1
+#define GS_DEBUG_INJECT_STALL 2
+#define GS_DEBUG_BUDGET       3
+gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* GPUSORT_GB300_H_ */

@@ -1,0 +1,158 @@
+"""Parity of the onesweep radix sort with the CPU oracle, through the C ABI.
+
+Bit-exact comparison for every key type of the reference's instantiation
+set (src/cuda_utils.cu:257-262), ascending (std::less) and descending
+(std::greater), over the reference's test distributions (src/test/utils.h:
+425-608) plus the adversarial ones of the sort workloads.
+"""
+import numpy as np
+import pytest
+
+from gpusort_gb300 import capi, datagen
+from oracle import oracle
+from tests._util import empty_dev, from_dev, same_bits, to_dev
+
+pytestmark = pytest.mark.gpu
+
+DTYPES = [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64]
+SMALL = [1, 2, 3, 31, 32, 33, 255, 256, 257, 1000, 6143, 6144, 6145, 8191, 8192, 8193, 40000]
+DISTS = ["uniform", "sorted", "reverse", "equal", "distinct8", "zipf"]
+
+
+def _sort(ctx, a, descending=False, in_place=False):
+    d_in = to_dev(a)
+    d_out = d_in if in_place else empty_dev(a.size, a.dtype)
+    st = ctx.sort_keys(d_in, d_out, dtype=a.dtype, descending=descending, flags=capi.FLAG_SYNC)
+    assert st == capi.GS_OK, ctx.last_error()
+    return from_dev(d_out, a.dtype)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("dist", DISTS)
+def test_keys_small_sizes(ctx, dtype, dist):
+    for i, n in enumerate(SMALL):
+        a = datagen.host(dist, n, dtype, seed=100 + i)
+        for desc in (False, True):
+            got = _sort(ctx, a, desc)
+            want = oracle.sort_keys(a, desc)
+            assert same_bits(got, want), (dtype, dist, n, desc)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [1 << 20, (1 << 22) + 12345])
+def test_keys_large_uniform(ctx, dtype, n):
+    a = datagen.host("uniform", n, dtype, seed=7)
+    for desc in (False, True):
+        assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc)), (dtype, n, desc)
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.uint64, np.float32])
+@pytest.mark.parametrize("dist", ["zipf", "distinct8", "equal", "sorted", "reverse"])
+def test_keys_large_adversarial(ctx, dtype, dist):
+    a = datagen.host(dist, (1 << 21) + 77, dtype, seed=11)
+    for desc in (False, True):
+        assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc)), (dtype, dist, desc)
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.float64, np.int32])
+@pytest.mark.parametrize("dist", ["uniform", "equal", "distinct8"])
+def test_keys_in_place(ctx, dtype, dist):
+    for n in (1, 100, 8193, 300001):
+        a = datagen.host(dist, n, dtype, seed=5)
+        for desc in (False, True):
+            assert same_bits(_sort(ctx, a, desc, in_place=True), oracle.sort_keys(a, desc))
+
+
+def test_keys_float_specials(ctx):
+    a = np.array([np.inf, -np.inf, 0.0, 1e-45, -1e-45, 3.4e38, -3.4e38, 1.0, -1.0, 2.5] * 1000,
+                 dtype=np.float32)
+    for desc in (False, True):
+        assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc))
+
+
+def test_keys_host_pointers(ctx):
+    a = datagen.host("uniform", 123457, np.uint32, seed=9)
+    out = np.empty_like(a)
+    st = ctx.sort_keys(a, out, flags=capi.FLAG_HOST)
+    assert st == capi.GS_OK, ctx.last_error()
+    assert same_bits(out, oracle.sort_keys(a))
+    b = a.copy()
+    st = ctx.sort_keys(b, b, flags=capi.FLAG_HOST, descending=True)
+    assert st == capi.GS_OK
+    assert same_bits(b, oracle.sort_keys(a, True))
+
+
+def test_empty_input_reports_empty(ctx):
+    a = np.empty(0, np.uint32)
+    st = ctx.sort_keys(a, a, flags=capi.FLAG_HOST)
+    assert st == capi.GS_ERR_EMPTY
+    assert ctx.last_error() == "No data to sort."
+
+
+PAIR_TYPES = [(np.uint32, np.uint32), (np.uint64, np.uint32), (np.float32, np.uint64),
+              (np.int64, np.uint32), (np.float64, np.float64), (np.int32, np.int64),
+              (np.uint32, np.float32), (np.uint64, np.uint64)]
+
+
+def _pairs(ctx, k, v, descending, stable, in_place=False):
+    dk, dv = to_dev(k), to_dev(v)
+    ok = dk if in_place else empty_dev(k.size, k.dtype)
+    ov = dv if in_place else empty_dev(v.size, v.dtype)
+    st = ctx.sort_pairs(dk, dv, ok, ov, key_dtype=k.dtype, val_dtype=v.dtype,
+                        descending=descending, stable=stable, flags=capi.FLAG_SYNC)
+    assert st == capi.GS_OK, ctx.last_error()
+    return from_dev(ok, k.dtype), from_dev(ov, v.dtype)
+
+
+@pytest.mark.parametrize("kt,vt", PAIR_TYPES)
+@pytest.mark.parametrize("stable", [False, True])
+def test_pairs(ctx, kt, vt, stable):
+    for i, n in enumerate([1, 33, 5000, 6145, 100003]):
+        for dist in ("distinct8", "uniform", "zipf"):
+            k = datagen.host(dist, n, kt, seed=i)
+            v = (np.arange(n, dtype=np.uint64).astype(vt) if stable
+                 else datagen.host("distinct8" if i % 2 else "uniform", n, vt, seed=i + 50))
+            for desc in (False, True):
+                gk, gv = _pairs(ctx, k, v, desc, stable, in_place=(i == 3))
+                wk, wv = oracle.sort_pairs(k, v, desc, stable)
+                assert same_bits(gk, wk) and same_bits(gv, wv), (kt, vt, n, dist, desc, stable)
+
+
+def test_pairs_stable_index_payload_large(ctx):
+    """(uint64 key, uint32 original index) pairs, Zipf keys: stable order."""
+    n = (1 << 21) + 3
+    k = datagen.host("zipf", n, np.uint64, seed=3)
+    v = np.arange(n, dtype=np.uint32)
+    for desc in (False, True):
+        gk, gv = _pairs(ctx, k, v, desc, True)
+        wk, wv = oracle.sort_pairs(k, v, desc, True)
+        assert same_bits(gk, wk) and same_bits(gv, wv)
+
+
+def test_lookback_wait_runs_out_and_context_recovers(ctx):
+    """A tile waits on a predecessor flag that is never set: the bounded
+    wait ends, the call reports GS_ERR_TIMEOUT, and the next sort is right."""
+    a = datagen.host("uniform", 200000, np.uint32, seed=1)
+    d_in, d_out = to_dev(a), empty_dev(a.size, np.uint32)
+    ctx.debug_set(capi.DEBUG_SPIN_LIMIT, 2000)
+    ctx.debug_set(capi.DEBUG_INJECT_STALL, 1)
+    st = ctx.sort_keys(d_in, d_out, dtype=np.uint32, flags=capi.FLAG_SYNC)
+    ctx.debug_set(capi.DEBUG_SPIN_LIMIT, 1 << 20)
+    assert st == capi.GS_ERR_TIMEOUT
+    assert "ran out" in ctx.last_error()
+    assert same_bits(_sort(ctx, a), oracle.sort_keys(a))
+
+
+def test_budget_exhausted_reports_oom(built_lib):
+    import torch
+    from gpusort_gb300 import Context
+    c = Context(0, hbm_budget_bytes=1 << 20)
+    try:
+        a = datagen.host("uniform", 1 << 20, np.uint32, seed=2)
+        d = to_dev(a)
+        st = c.sort_keys(d, d, dtype=np.uint32, flags=capi.FLAG_SYNC)
+        assert st == capi.GS_ERR_OOM
+        assert "budget" in c.last_error()
+        torch.cuda.synchronize()
+    finally:
+        c.close()
