@@ -46,7 +46,7 @@ EXPORTED = [
     "gs_ctx_set_stream", "gs_ctx_synchronize", "gs_last_error",
     "gs_last_global_error", "gs_sort_keys", "gs_sort_pairs",
     "gs_segmented_sort_keys", "gs_gather", "gs_phase_times",
-    "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set",
+    "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set", "gs_sort_keys_noalloc",
 ]
 
 _NP_DTYPE = {
@@ -110,6 +110,8 @@ def load() -> C.CDLL:
         L.gs_kernel_times.argtypes = [vp, C.POINTER(C.c_double), i32]
         L.gs_kernel_times.restype = i32
         L.gs_debug_set.argtypes = [vp, i32, u64]
+        L.gs_sort_keys_noalloc.argtypes = [i32, vp, vp, u64, u32, vp]
+        L.gs_sort_keys_noalloc.restype = i32
         for fn in ("gs_ctx_set_stream", "gs_ctx_synchronize", "gs_sort_keys", "gs_sort_pairs",
                    "gs_segmented_sort_keys", "gs_gather", "gs_ctx_set_timing", "gs_debug_set"):
             getattr(L, fn).restype = i32

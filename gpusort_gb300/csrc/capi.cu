@@ -20,6 +20,10 @@ struct DevBuf {
 
 }  // namespace
 
+namespace gs {
+void set_last_global_error(const std::string& msg) { g_last_global_error = msg; }
+}  // namespace gs
+
 struct gs_ctx {
   gs::DeviceProps props;
   cudaStream_t own_stream = nullptr;

@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace gs {
@@ -48,6 +49,9 @@ uint32_t radix_tile(int key_bytes, int val_bytes);
 // Look-back words a job of n elements needs.
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
 size_t sort_work_bytes();
+
+// Set the message gs_last_global_error() returns on this thread.
+void set_last_global_error(const std::string& msg);
 
 // Enqueue the whole radix pipeline on `stream`. `gen` is the context's
 // launch-generation counter (advanced once per pass launch); the caller

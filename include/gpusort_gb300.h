@@ -190,6 +190,27 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
 #define GS_DEBUG_BUDGET       3
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
+/* Sort 32-bit keys (GS_U32, GS_I32, GS_F32) in device memory WITHOUT
+ * ALLOCATING. No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc - code running under a framework whose caching
+ * allocator owns the device memory, latency-critical paths where
+ * cudaMalloc/cudaFree would synchronise the device, plugins whose host
+ * forbids allocation after start-up.
+ * - Scratch is one fixed device array inside the library (about 4.3 MB per
+ *   GPU that loads it, held until the process exits). n may be at most
+ *   GS_NOALLOC_MAX_KEYS; larger n returns GS_ERR_TOO_LARGE.
+ * - The caller passes device input and output (they may alias) and a CUDA
+ *   stream (NULL: the legacy default stream). Flags: GS_FLAG_DESCENDING,
+ *   and GS_FLAG_SYNC to wait and report GS_ERR_TIMEOUT.
+ * - The first call on a device sets up that device's scratch address (and
+ *   clears it); make that first call before any stream capture.
+ * - Every call on a device shares the one scratch array: calls that overlap
+ *   on the GPU (other streams, other threads) race and corrupt each other.
+ * - Errors are described by gs_last_global_error(). */
+#define GS_NOALLOC_MAX_KEYS (1ull << 20)
+gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out,
+                               uint64_t n, uint32_t flags, void* stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
