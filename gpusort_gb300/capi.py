@@ -39,6 +39,7 @@ ALGO_AUTO, ALGO_RADIX, ALGO_SAMPLE, ALGO_HYK = range(4)
 DEBUG_SPIN_LIMIT = 1
 DEBUG_INJECT_STALL = 2
 DEBUG_BUDGET = 3
+DEBUG_PASS_SHAPE = 4
 
 # Every symbol include/gpusort_gb300.h declares (checked by the CPU tests).
 EXPORTED = [

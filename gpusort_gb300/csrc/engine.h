@@ -33,6 +33,7 @@ struct RadixJob {
   bool desc = false;
   bool ties_by_value = false;       // value digits take part in the order
   bool reverse_first = false;       // stable descending pairs
+  bool first_unstable = false;      // no ties to keep: first pass may be unstable
   uint64_t* status = nullptr;       // radix_status_words(n, ...) words
   SortWork* work = nullptr;
   uint32_t* err = nullptr;
@@ -42,10 +43,15 @@ struct RadixJob {
   // pipeline (marks[0]), after the upsweep (1), after the plan (2) and after
   // each pass q (3 + q). Needs 3 + digits events.
   cudaEvent_t* marks = nullptr;
+  int shape = 0;                    // pass-kernel tile shape (0 .. radix_num_shapes()-1)
 };
 
-// Tile size (elements) of the pass kernel for a key/value width pair.
+// Smallest tile (elements) of the pass kernel over all shapes: sizes the
+// look-back words.
 uint32_t radix_tile(int key_bytes, int val_bytes);
+int radix_num_shapes();
+// Look-back words of a 32-bit keys-only job run with the default shape.
+size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
 size_t sort_work_bytes();

@@ -86,7 +86,7 @@ gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out, uint64
                                       " exceeds its fixed scratch limit of " +
                                       std::to_string(kMaxKeys) + " keys");
   if (!in || !out) return fail(GS_ERR_INVALID, "null data pointer");
-  if (gs::radix_status_words(n, 4, 0) * sizeof(uint64_t) > kStatusBytes)
+  if (gs::radix_status_words_u32_shape0(n) * sizeof(uint64_t) > kStatusBytes)
     return fail(GS_ERR_INVALID, "gs_sort_keys_noalloc: look-back area too small");
   if (flags & GS_FLAG_HOST)
     return fail(GS_ERR_INVALID, "gs_sort_keys_noalloc takes device pointers only");

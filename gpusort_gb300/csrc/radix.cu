@@ -8,22 +8,33 @@ namespace {
 
 constexpr int UPSWEEP_THREADS = 512;
 constexpr int UPSWEEP_UNROLL = 8;
-constexpr int PASS_THREADS = 512;
 
-// Items per thread of the pass kernel, by bytes per element (key + value).
-template <typename K, typename V> struct PassItems;
-template <> struct PassItems<uint32_t, NoValue> { static constexpr int v = 16; };
-template <> struct PassItems<uint64_t, NoValue> { static constexpr int v = 12; };
-template <> struct PassItems<uint32_t, uint32_t> { static constexpr int v = 12; };
-template <> struct PassItems<uint32_t, uint64_t> { static constexpr int v = 8; };
-template <> struct PassItems<uint64_t, uint32_t> { static constexpr int v = 8; };
-template <> struct PassItems<uint64_t, uint64_t> { static constexpr int v = 8; };
+// Tile shapes of the pass kernel (threads per block, items per thread,
+// blocks per SM), selectable per call; shape 0 is the default. Larger
+// elements take fewer items per thread.
+template <int T, int I, int B> struct Shape {
+  static constexpr int THREADS = T, ITEMS = I, MINB = B;
+};
+template <typename K, typename V, int S> struct PassShape;
+template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 16, 2> {};
+template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 16, 4> {};
+template <> struct PassShape<uint32_t, NoValue, 2> : Shape<256, 24, 4> {};
+template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 12, 2> {};
+template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4> {};
+template <> struct PassShape<uint64_t, NoValue, 2> : Shape<256, 16, 4> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 12, 2> {};
+template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4> {};
+template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 16, 4> {};
+template <typename K, typename V, int S> struct PassShape : Shape<(S == 0 ? 512 : 256), 8, (S == 0 ? 2 : 4)> {};
+constexpr int NUM_SHAPES = 3;
+constexpr uint32_t MIN_TILE = 256 * 8;  // smallest tile of any shape
 
-template <typename K, typename V>
+template <typename K, typename V, int S>
 cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
                 cudaStream_t stream) {
-  constexpr int ITEMS = PassItems<K, V>::v;
-  constexpr int MINB = 2;
+  constexpr int PASS_THREADS = PassShape<K, V, S>::THREADS;
+  constexpr int ITEMS = PassShape<K, V, S>::ITEMS;
+  constexpr int MINB = PassShape<K, V, S>::MINB;
   using Cfg = PassConfig<K, V, PASS_THREADS, ITEMS>;
   constexpr bool HAS_V = Cfg::HAS_V;
   const uint32_t kd = Bits<K>::DIGITS;
@@ -85,6 +96,7 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   pa.val_kind = job.val_kind;
   pa.desc = job.desc;
   pa.reverse_first = job.reverse_first;
+  pa.first_unstable = job.first_unstable && !job.reverse_first;
   pa.status = job.status;
   pa.spin_limit = job.spin_limit;
   pa.inject_stall = job.inject_stall;
@@ -102,28 +114,45 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
 }  // namespace
 
 uint32_t radix_tile(int key_bytes, int val_bytes) {
-  if (key_bytes == 4 && val_bytes == 0) return PASS_THREADS * PassItems<uint32_t, NoValue>::v;
-  if (key_bytes == 8 && val_bytes == 0) return PASS_THREADS * PassItems<uint64_t, NoValue>::v;
-  if (key_bytes == 4 && val_bytes == 4) return PASS_THREADS * PassItems<uint32_t, uint32_t>::v;
-  return PASS_THREADS * 8;
+  (void)key_bytes;
+  (void)val_bytes;
+  return MIN_TILE;
 }
+
+int radix_num_shapes() { return NUM_SHAPES; }
 
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes) {
   const uint64_t t = radix_tile(key_bytes, val_bytes);
   return size_t((n + t - 1) / t) * RADIX;
 }
 
+size_t radix_status_words_u32_shape0(uint64_t n) {
+  constexpr uint64_t t = uint64_t(PassShape<uint32_t, NoValue, 0>::THREADS) *
+                         PassShape<uint32_t, NoValue, 0>::ITEMS;
+  return size_t((n + t - 1) / t) * RADIX;
+}
+
 size_t sort_work_bytes() { return sizeof(SortWork); }
+
+template <typename K, typename V>
+cudaError_t run_shape(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
+                      cudaStream_t stream) {
+  switch (job.shape) {
+    case 1: return run<K, V, 1>(job, props, gen, stream);
+    case 2: return run<K, V, 2>(job, props, gen, stream);
+    default: return run<K, V, 0>(job, props, gen, stream);
+  }
+}
 
 cudaError_t launch_radix_sort(const RadixJob& job, const DeviceProps& props,
                               uint32_t* gen, cudaStream_t stream) {
   const int kb = job.key_bytes, vb = job.val_bytes;
-  if (kb == 4 && vb == 0) return run<uint32_t, NoValue>(job, props, gen, stream);
-  if (kb == 8 && vb == 0) return run<uint64_t, NoValue>(job, props, gen, stream);
-  if (kb == 4 && vb == 4) return run<uint32_t, uint32_t>(job, props, gen, stream);
-  if (kb == 4 && vb == 8) return run<uint32_t, uint64_t>(job, props, gen, stream);
-  if (kb == 8 && vb == 4) return run<uint64_t, uint32_t>(job, props, gen, stream);
-  if (kb == 8 && vb == 8) return run<uint64_t, uint64_t>(job, props, gen, stream);
+  if (kb == 4 && vb == 0) return run_shape<uint32_t, NoValue>(job, props, gen, stream);
+  if (kb == 8 && vb == 0) return run_shape<uint64_t, NoValue>(job, props, gen, stream);
+  if (kb == 4 && vb == 4) return run_shape<uint32_t, uint32_t>(job, props, gen, stream);
+  if (kb == 4 && vb == 8) return run_shape<uint32_t, uint64_t>(job, props, gen, stream);
+  if (kb == 8 && vb == 4) return run_shape<uint64_t, uint32_t>(job, props, gen, stream);
+  if (kb == 8 && vb == 8) return run_shape<uint64_t, uint64_t>(job, props, gen, stream);
   return cudaErrorInvalidValue;
 }
 

@@ -10,10 +10,12 @@
 //   2. plan_kernel     - exclusive scans of those histograms (global bin
 //                        bases), skip decisions for digits whose histogram
 //                        has a single non-empty bin, ping-pong buffer plan;
-//   3. pass_kernel x D - one pass per digit: warp match_any ranking, tile
-//                        aggregate published at once, decoupled look-back
-//                        across tiles with bounded waits, tile reordered in
-//                        shared memory, coalesced scatter by digit.
+//   3. pass_kernel x D - one pass per digit: stable warp ranking through
+//                        shared peer masks (the first pass may use one shared
+//                        atomic per element instead), tile aggregate
+//                        published at once, windowed decoupled look-back with
+//                        bounded waits, tile reordered in shared memory,
+//                        coalesced scatter by digit.
 // Everything is enqueued on one stream without host round trips, so the
 // pipeline is graph-capturable.
 #pragma once
@@ -27,16 +29,10 @@ namespace gs {
 // Upsweep: all digit histograms in one read.
 // ---------------------------------------------------------------------------
 
-// Count digit `d` in histogram `h`. When the whole warp holds the same digit
-// (sorted runs, all-equal or low-cardinality inputs) one lane adds 32, so a
-// skewed input does not serialise on one shared-memory word.
+// Count digit `d` in histogram `h`. Shared atomics to one address from a
+// whole warp are combined in hardware, so skewed inputs need no special case.
 __device__ __forceinline__ void add_digit(uint32_t* h, uint32_t d, bool valid) {
-  const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-  if (__all_sync(0xffffffffu, valid && d == d0)) {
-    if ((threadIdx.x & 31) == 0) atomicAdd(&h[d0], 32u);
-  } else if (valid) {
-    atomicAdd(&h[d], 1u);
-  }
+  if (valid) atomicAdd(&h[d], 1u);
 }
 
 template <typename K, typename V, int THREADS, int UNROLL>
@@ -153,6 +149,7 @@ template <typename K, typename V, int THREADS, int ITEMS>
 struct PassConfig {
   static constexpr int WARPS = THREADS / 32;
   static constexpr int TILE = THREADS * ITEMS;
+  static_assert(TILE <= 65536, "ranks are packed as 16-bit fields");
   static constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
   static constexpr size_t VAL_BYTES = HAS_V ? sizeof(typename std::conditional<HAS_V, V, uint32_t>::type) : 0;
   static constexpr size_t SMEM_KEYS = size_t(TILE) * sizeof(K);
@@ -160,6 +157,31 @@ struct PassConfig {
   static constexpr size_t DYN_SMEM = SMEM_KEYS + SMEM_VALS;
 };
 
+// Branch-free order transform of one element type: forward maps raw bits
+// to bits whose unsigned order is the requested order; inverse undoes it.
+template <typename U>
+struct OrderXform {
+  U fmask, smask, dmask;
+  __device__ __forceinline__ OrderXform(uint32_t kind, bool desc)
+      : fmask(kind == KIND_FLOAT ? ~U(0) : U(0)),
+        smask(kind == KIND_UNSIGNED ? U(0) : Bits<U>::SIGN),
+        dmask(desc ? ~U(0) : U(0)) {}
+  __device__ __forceinline__ U fwd(U x) const {
+    using S = typename std::make_signed<U>::type;
+    const U neg = U(S(x) >> (8 * sizeof(U) - 1));
+    return x ^ ((neg & fmask) | smask) ^ dmask;
+  }
+  __device__ __forceinline__ U inv(U y) const {
+    using S = typename std::make_signed<U>::type;
+    const U t = y ^ dmask;
+    const U was_neg = U(S(~t) >> (8 * sizeof(U) - 1));
+    return t ^ ((was_neg & fmask) | smask);
+  }
+};
+
+// Keys live in the transformed domain between passes: the first pass that
+// runs transforms them on load, the last one restores raw bits on store.
+// Values stay raw and are transformed only to extract a value digit.
 template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 pass_kernel(PassParams p) {
@@ -167,11 +189,15 @@ pass_kernel(PassParams p) {
   constexpr int WARPS = Cfg::WARPS;
   constexpr int TILE = Cfg::TILE;
   constexpr bool HAS_V = Cfg::HAS_V;
+  constexpr int LB_WIN = 8;  // look-back words read per round
   using VS = typename std::conditional<HAS_V, V, uint32_t>::type;  // storage type
 
   extern __shared__ __align__(16) uint8_t s_dyn[];
-  __shared__ uint32_t s_warp_hist[WARPS][RADIX + 1];
-  __shared__ uint32_t s_tile_excl[RADIX];
+  // Stable ranking: per warp and digit, [31:0] peer mask of the current
+  // item row, [63:32] running count. After ranking, [31:0] becomes the
+  // digit's start in the tile for that warp. The unstable ranking uses the
+  // first RADIX+1 words as tile counters, later tile offsets.
+  __shared__ uint64_t s_tab[WARPS][RADIX + 1];
   __shared__ uint32_t s_dst_base[RADIX];
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
@@ -180,13 +206,15 @@ pass_kernel(PassParams p) {
   const uint32_t j = plan.exec_index[p.pass];
   if (j == PASS_SKIPPED) return;
   const uint32_t m = plan.m_exec;
+  const bool first = (j == 0);
+  const bool last = (j + 1 == m);
 
   // Ping-pong: pass j writes `out` when (m - j) is odd, so the last pass
   // always lands in `out`; pass 0 reads the caller's input.
   const bool dst_is_out = ((m - j) & 1u) != 0;
   const K* src_k;
   const VS* src_v = nullptr;
-  if (j == 0) {
+  if (first) {
     src_k = static_cast<const K*>(p.keys_in);
     if constexpr (HAS_V) src_v = static_cast<const VS*>(p.vals_in);
   } else {
@@ -196,130 +224,188 @@ pass_kernel(PassParams p) {
   K* dst_k = static_cast<K*>(dst_is_out ? p.keys_out : p.keys_alt);
   VS* dst_v = nullptr;
   if constexpr (HAS_V) dst_v = static_cast<VS*>(dst_is_out ? p.vals_out : p.vals_alt);
-  const bool reverse = (j == 0) && p.reverse_first;
+  const bool reverse = first && p.reverse_first;
+  // The first pass that runs may order equal digits arbitrarily when the
+  // requested order leaves no ties to preserve (keys only, or pairs ordered
+  // by value too): equal digits there are either equal in every later digit
+  // (identical elements) or separated by a later, stable pass.
+  const bool unstable = first && p.first_unstable;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
   const uint64_t n = p.n;
-  const bool desc = p.desc != 0;
   const bool from_val = p.pass < p.val_digits;
   const uint32_t shift = RADIX_BITS * (from_val ? p.pass : (p.pass - p.val_digits));
+  const OrderXform<K> kx(p.key_kind, p.desc != 0);
+  const OrderXform<VS> vx(p.val_kind, p.desc != 0);
 
   if (tid == 0) s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
-  for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&s_warp_hist[0][0])[i] = 0;
+  {
+    uint4* z = reinterpret_cast<uint4*>(&s_tab[0][0]);
+    constexpr int Z = WARPS * (RADIX + 1) / 2;
+    for (int i = tid; i < Z; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
+  }
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint64_t tile_base = uint64_t(tile) * TILE;
-  const uint64_t warp_base = tile_base + uint64_t(warp) * 32 * ITEMS;
+  const uint64_t remaining = n - tile_base;
+  const uint32_t tile_n = remaining < uint64_t(TILE) ? uint32_t(remaining) : uint32_t(TILE);
+  const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
 
-  auto digit_of_key = [&](K k) -> uint32_t {
-    return uint32_t(order_bits<K>(k, p.key_kind, desc) >> shift) & (RADIX - 1);
-  };
-  auto digit_of_val = [&](VS v) -> uint32_t {
-    return uint32_t(order_bits<VS>(v, p.val_kind, desc) >> shift) & (RADIX - 1);
-  };
-
-  // Load: item i of lane l is element warp_base + 32*i + l, so (i, lane)
-  // order is input order and the ranking below is stable.
+  // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
+  // is input order and the stable ranking below keeps it.
   K keys[ITEMS];
   VS vals[HAS_V ? ITEMS : 1];
-  uint32_t rank[ITEMS];
+  if (!reverse) {
+    const K* sk = src_k + tile_base + wloc;
+    const VS* sv = nullptr;
+    if constexpr (HAS_V) sv = src_v + tile_base + wloc;
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const uint64_t idx = warp_base + uint64_t(i) * 32 + lane;
-    const bool valid = idx < n;
-    const uint64_t sidx = reverse ? (n - 1 - idx) : idx;
-    keys[i] = valid ? ld_stream(src_k + sidx) : K(0);
-    if constexpr (HAS_V) vals[i] = valid ? ld_stream(src_v + sidx) : VS(0);
-  }
-
-  // Warp ranking with match_any: peers holding the same digit get
-  // consecutive ranks in lane order; the group's lowest lane bumps the
-  // warp's counter for that digit.
-  const uint32_t lt = lanemask_lt();
-  uint32_t* wh = s_warp_hist[warp];
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const uint64_t idx = warp_base + uint64_t(i) * 32 + lane;
-    uint32_t d;
-    if constexpr (HAS_V) {
-      d = from_val ? digit_of_val(vals[i]) : digit_of_key(keys[i]);
-    } else {
-      d = digit_of_key(keys[i]);
+    for (int i = 0; i < ITEMS; ++i) {
+      const bool valid = wloc + 32 * i < tile_n;
+      keys[i] = valid ? ld_stream(sk + 32 * i) : K(0);
+      if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv + 32 * i) : VS(0);
     }
-    d = (idx < n) ? d : uint32_t(RADIX);  // padding lanes use the spare bin
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t base = wh[d];
-    rank[i] = base + __popc(peers & lt);
-    __syncwarp();
-    if ((peers & lt) == 0) wh[d] = base + __popc(peers);
-    __syncwarp();
+  } else {
+    const K* sk = src_k + (n - 1 - tile_base - wloc);
+    const VS* sv = nullptr;
+    if constexpr (HAS_V) sv = src_v + (n - 1 - tile_base - wloc);
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const bool valid = wloc + 32 * i < tile_n;
+      keys[i] = valid ? ld_stream(sk - 32 * i) : K(0);
+      if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv - 32 * i) : VS(0);
+    }
+  }
+  if (first) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) keys[i] = kx.fwd(keys[i]);
+  }
+  auto digit_at = [&](int i) -> uint32_t {
+    if constexpr (HAS_V) {
+      if (from_val) return uint32_t(vx.fwd(vals[i]) >> shift) & (RADIX - 1);
+    }
+    return uint32_t(keys[i] >> shift) & (RADIX - 1);
+  };
+
+  // Ranks are below the tile size (< 2^16): two per register.
+  uint32_t rank2[(ITEMS + 1) / 2];
+#pragma unroll
+  for (int i = 0; i < (ITEMS + 1) / 2; ++i) rank2[i] = 0;
+  auto set_rank = [&](int i, uint32_t r) { rank2[i >> 1] |= r << (16 * (i & 1)); };
+  auto get_rank = [&](int i) -> uint32_t { return (rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu; };
+
+  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(&s_tab[0][0]);
+  if (unstable) {
+    // One shared atomic per element: its rank among the tile's elements of
+    // the same digit, in no particular order.
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      if (wloc + 32 * i < tile_n) set_rank(i, atomicAdd(&s_cnt[digit_at(i)], 1u));
+    }
+  } else {
+    // Stable warp ranking: each lane sets its bit in the digit's peer mask,
+    // reads back the mask and the digit's running count; the group's lowest
+    // lane advances the count and clears the mask.
+    const uint32_t lt = lanemask_lt();
+    const uint32_t bit = 1u << lane;
+    uint64_t* tab = s_tab[warp];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const uint32_t d = (wloc + 32 * i < tile_n) ? digit_at(i) : uint32_t(RADIX);
+      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]), bit);
+      __syncwarp();
+      const uint64_t e = tab[d];
+      __syncwarp();
+      const uint32_t peers = uint32_t(e);
+      const uint32_t below = peers & lt;
+      const uint32_t base = uint32_t(e >> 32);
+      set_rank(i, base + __popc(below));
+      if (below == 0) tab[d] = uint64_t(base + __popc(peers)) << 32;
+      __syncwarp();
+    }
   }
   __syncthreads();
 
-  // Per digit: exclusive offsets of each warp, tile count, aggregate out.
+  // Per digit: tile count, per-warp exclusive offsets (stable), aggregate
+  // published at once.
   uint32_t count = 0;
   uint64_t* status = p.status + uint64_t(tile) * RADIX;
   if (tid < RADIX) {
-    uint32_t run = 0;
+    if (unstable) {
+      count = s_cnt[tid];
+    } else {
+      uint32_t run = 0;
 #pragma unroll
-    for (int w = 0; w < WARPS; ++w) {
-      const uint32_t c = s_warp_hist[w][tid];
-      s_warp_hist[w][tid] = run;
-      run += c;
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = uint32_t(s_tab[w][tid] >> 32);
+        s_tab[w][tid] = run;  // this thread owns column tid
+        run += c;
+      }
+      count = run;
     }
-    count = run;
     st_relaxed(status + tid, make_status(tile == 0 ? FLAG_INC : FLAG_AGG, p.gen, count));
   }
   const uint32_t tile_excl = block_excl_scan_256(count, s_tmp);
 
-  // Decoupled look-back over preceding tiles, bounded.
+  // Decoupled look-back over preceding tiles, LB_WIN words per round,
+  // bounded by spin_limit rounds without progress.
   if (tid < RADIX) {
     uint32_t prefix = 0;
     if (tile > 0) {
       int64_t t = int64_t(tile) - 1;
-      uint32_t spins = 0;
-      uint32_t backoff = 8;
+      uint32_t idle_rounds = 0;
       const bool stall = p.inject_stall && tile == 1;
+      const uint32_t gen = p.gen & GEN_MASK;
       while (true) {
-        const uint64_t w = stall ? 0ull : ld_relaxed(p.status + uint64_t(t) * RADIX + tid);
-        const uint64_t flag = w & FLAG_MASK;
-        if (flag == 0 || uint32_t(w >> 32 & GEN_MASK) != (p.gen & GEN_MASK)) {
-          if (++spins > p.spin_limit) {
-            atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
-            break;
-          }
-          __nanosleep(backoff);
-          if (backoff < 1024) backoff <<= 1;
-          continue;
+        uint64_t w[LB_WIN];
+#pragma unroll
+        for (int k = 0; k < LB_WIN; ++k) {
+          const int64_t tt = t - k;
+          w[k] = (tt >= 0 && !stall) ? ld_relaxed(p.status + uint64_t(tt) * RADIX + tid) : 0ull;
         }
-        prefix += uint32_t(w);
-        if (flag == FLAG_INC || t == 0) break;
-        --t;
-        backoff = 8;
+        int consumed = 0;
+        bool done = false;
+#pragma unroll
+        for (int k = 0; k < LB_WIN; ++k) {
+          const uint64_t wk = w[k];
+          const bool ready = (wk & FLAG_MASK) != 0 && uint32_t((wk >> 32) & GEN_MASK) == gen;
+          if (!done && consumed == k && ready) {
+            prefix += uint32_t(wk);
+            consumed = k + 1;
+            done = (wk & FLAG_MASK) == FLAG_INC;
+          }
+        }
+        if (done) break;
+        t -= consumed;
+        if (consumed == 0 && ++idle_rounds > p.spin_limit) {
+          atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
+          break;
+        }
       }
       st_relaxed(status + tid, make_status(FLAG_INC, p.gen, prefix + count));
     }
-    s_tile_excl[tid] = tile_excl;
     s_dst_base[tid] = plan.binbase[p.pass][tid] + prefix - tile_excl;
+    if (unstable) {
+      s_cnt[tid] = tile_excl;
+    } else {
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) s_tab[w][tid] += tile_excl;
+    }
   }
   __syncthreads();
 
-  // Reorder the tile in shared memory by digit.
+  // Reorder the tile in shared memory by digit (keys in transformed form).
   K* s_keys = reinterpret_cast<K*>(s_dyn);
   VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
+  const uint32_t* s_off = reinterpret_cast<const uint32_t*>(&s_tab[warp][0]);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
-    const uint64_t idx = warp_base + uint64_t(i) * 32 + lane;
-    if (idx < n) {
-      uint32_t d;
-      if constexpr (HAS_V) {
-        d = from_val ? digit_of_val(vals[i]) : digit_of_key(keys[i]);
-      } else {
-        d = digit_of_key(keys[i]);
-      }
-      const uint32_t pos = s_tile_excl[d] + s_warp_hist[warp][d] + rank[i];
+    if (wloc + 32 * i < tile_n) {
+      const uint32_t d = digit_at(i);
+      const uint32_t start = unstable ? s_cnt[d] : s_off[2 * d];
+      const uint32_t pos = start + get_rank(i);
       s_keys[pos] = keys[i];
       if constexpr (HAS_V) s_vals[pos] = vals[i];
     }
@@ -328,8 +414,7 @@ pass_kernel(PassParams p) {
 
   // Scatter: consecutive tile positions of one digit go to consecutive
   // output addresses.
-  const uint64_t remaining = n - tile_base;
-  const uint32_t tile_n = remaining < uint64_t(TILE) ? uint32_t(remaining) : uint32_t(TILE);
+  const uint32_t n32 = uint32_t(n);  // n < 2^32
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     const uint32_t r = uint32_t(i) * THREADS + tid;
@@ -339,13 +424,14 @@ pass_kernel(PassParams p) {
       VS v;
       if constexpr (HAS_V) {
         v = s_vals[r];
-        d = from_val ? digit_of_val(v) : digit_of_key(k);
+        d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1))
+                     : (uint32_t(k >> shift) & (RADIX - 1));
       } else {
-        d = digit_of_key(k);
+        d = uint32_t(k >> shift) & (RADIX - 1);
       }
       const uint32_t dst = s_dst_base[d] + r;
-      if (uint64_t(dst) < n) {
-        dst_k[dst] = k;
+      if (dst < n32) {
+        dst_k[dst] = last ? kx.inv(k) : k;
         if constexpr (HAS_V) dst_v[dst] = v;
       } else {
         atomicOr(p.err, ERR_SCATTER_RANGE);

@@ -50,6 +50,7 @@ struct PassParams {
   uint32_t key_kind, val_kind;
   uint32_t desc;
   uint32_t reverse_first;
+  uint32_t first_unstable;  // the first pass that runs may rank unstably
   uint64_t* status;       // num_tiles * RADIX look-back words
   uint32_t gen;
   uint32_t spin_limit;

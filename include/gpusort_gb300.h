@@ -184,10 +184,13 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
  * GS_DEBUG_INJECT_STALL: when non-zero, one tile of the next sort waits for
  * a predecessor flag that is never set, so the wait runs out after the spin
  * limit and the call reports GS_ERR_TIMEOUT.
- * GS_DEBUG_BUDGET: replace the HBM budget (bytes). */
+ * GS_DEBUG_BUDGET: replace the HBM budget (bytes).
+ * GS_DEBUG_PASS_SHAPE: tile shape of the radix pass kernel (threads x items
+ * per thread x blocks per SM); the autotuner sets it. */
 #define GS_DEBUG_SPIN_LIMIT   1
 #define GS_DEBUG_INJECT_STALL 2
 #define GS_DEBUG_BUDGET       3
+#define GS_DEBUG_PASS_SHAPE   4  /* pass-kernel tile shape 0..2 (tuning) */
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
 /* Sort 32-bit keys (GS_U32, GS_I32, GS_F32) in device memory WITHOUT

@@ -156,3 +156,25 @@ def test_budget_exhausted_reports_oom(built_lib):
         torch.cuda.synchronize()
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2])
+@pytest.mark.parametrize("kt,vt", [(np.uint32, None), (np.uint64, None), (np.float32, np.uint32),
+                                   (np.int64, np.uint64)])
+def test_every_tile_shape(ctx, shape, kt, vt):
+    """Each pass-kernel tile shape the autotuner may pick gives the same bytes."""
+    ctx.debug_set(capi.DEBUG_PASS_SHAPE, shape)
+    try:
+        for n in (1, 777, 8193, 100003, 1 << 20):
+            k = datagen.host("uniform" if n % 2 else "distinct8", n, kt, seed=n + shape)
+            if vt is None:
+                for desc in (False, True):
+                    assert same_bits(_sort(ctx, k, desc), oracle.sort_keys(k, desc))
+            else:
+                v = datagen.host("uniform", n, vt, seed=n + 1)
+                for stable in (False, True):
+                    gk, gv = _pairs(ctx, k, v, True, stable)
+                    wk, wv = oracle.sort_pairs(k, v, True, stable)
+                    assert same_bits(gk, wk) and same_bits(gv, wv)
+    finally:
+        ctx.debug_set(capi.DEBUG_PASS_SHAPE, 0)
