@@ -35,7 +35,7 @@ struct gs_ctx {
   uint32_t gen = 0;
   uint32_t spin_limit = 1u << 20;
   uint32_t inject_stall = 0;
-  int shape = 0;          // pass-kernel tile shape (tuning)
+  int shape = -1;         // pass-kernel tile shape (tuning); -1: per-type default
   bool timing = false;
   gs::SortWork* work = nullptr;
   uint32_t* err = nullptr;
@@ -180,7 +180,7 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
   job.err = ctx->err;
   job.spin_limit = ctx->spin_limit;
   job.inject_stall = ctx->inject_stall;
-  job.shape = ctx->shape;
+  job.shape = ctx->shape >= 0 ? ctx->shape : gs::radix_default_shape(kb, vb);
   ctx->inject_stall = 0;
 
   gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
@@ -440,7 +440,8 @@ gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value) {
     case GS_DEBUG_SPIN_LIMIT: ctx->spin_limit = value ? uint32_t(value) : 1u; return GS_OK;
     case GS_DEBUG_INJECT_STALL: ctx->inject_stall = value ? 1u : 0u; return GS_OK;
     case GS_DEBUG_BUDGET: ctx->budget = value; return GS_OK;
-    case GS_DEBUG_PASS_SHAPE:
+    case GS_DEBUG_PASS_SHAPE:  // UINT64_MAX restores the per-type defaults
+      if (value == ~0ull) { ctx->shape = -1; return GS_OK; }
       if (value >= uint64_t(gs::radix_num_shapes())) return fail(ctx, GS_ERR_INVALID, "bad shape");
       ctx->shape = int(value);
       return GS_OK;

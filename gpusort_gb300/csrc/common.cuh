@@ -20,7 +20,8 @@ enum KeyKind : uint32_t { KIND_UNSIGNED = 0, KIND_SIGNED = 1, KIND_FLOAT = 2 };
 enum ErrBits : uint32_t {
   ERR_LOOKBACK_TIMEOUT = 1u,
   ERR_SCATTER_RANGE = 2u,
-  ERR_COPY_TIMEOUT = 4u
+  ERR_COPY_TIMEOUT = 4u,
+  ERR_SMEM_ALIGN = 8u
 };
 
 struct NoValue {};

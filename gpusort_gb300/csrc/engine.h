@@ -50,6 +50,7 @@ struct RadixJob {
 // look-back words.
 uint32_t radix_tile(int key_bytes, int val_bytes);
 int radix_num_shapes();
+int radix_default_shape(int key_bytes, int val_bytes);
 // Look-back words of a 32-bit keys-only job run with the default shape.
 size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.

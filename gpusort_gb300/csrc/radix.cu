@@ -12,20 +12,26 @@ constexpr int UPSWEEP_UNROLL = 8;
 // Tile shapes of the pass kernel (threads per block, items per thread,
 // blocks per SM), selectable per call; shape 0 is the default. Larger
 // elements take fewer items per thread.
-template <int T, int I, int B> struct Shape {
-  static constexpr int THREADS = T, ITEMS = I, MINB = B;
+template <int T, int I, int B, int C = 8> struct Shape {
+  static constexpr int THREADS = T, ITEMS = I, MINB = B, CLUSTER = C;
 };
 template <typename K, typename V, int S> struct PassShape;
-template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 16, 2> {};
-template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 16, 4> {};
-template <> struct PassShape<uint32_t, NoValue, 2> : Shape<256, 24, 4> {};
-template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 12, 2> {};
-template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4> {};
-template <> struct PassShape<uint64_t, NoValue, 2> : Shape<256, 16, 4> {};
-template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 12, 2> {};
-template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4> {};
-template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 16, 4> {};
-template <typename K, typename V, int S> struct PassShape : Shape<(S == 0 ? 512 : 256), 8, (S == 0 ? 2 : 4)> {};
+// Shape 2 of keys-only sorts uses thread-block clusters (one look-back per
+// 8 tiles); it measured slower than per-tile look-back on GB300 and is kept
+// selectable for tuning. Key/value sorts never use clusters: a clustered
+// 256-thread pair variant raised an illegal-instruction fault on GB300
+// whose cause is not yet understood.
+template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 16, 2, 1> {};
+template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 24, 4, 1> {};
+template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 16, 2, 8> {};
+template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 12, 2, 1> {};
+template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 16, 4, 1> {};
+template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 12, 2, 8> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 12, 2, 1> {};
+template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4, 1> {};
+template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 16, 4, 1> {};
+template <typename K, typename V, int S>
+struct PassShape : Shape<(S == 0 ? 512 : 256), 8, (S == 0 ? 2 : 4), 1> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 256 * 8;  // smallest tile of any shape
 
@@ -35,6 +41,7 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   constexpr int PASS_THREADS = PassShape<K, V, S>::THREADS;
   constexpr int ITEMS = PassShape<K, V, S>::ITEMS;
   constexpr int MINB = PassShape<K, V, S>::MINB;
+  constexpr int CLUSTER = PassShape<K, V, S>::CLUSTER;
   using Cfg = PassConfig<K, V, PASS_THREADS, ITEMS>;
   constexpr bool HAS_V = Cfg::HAS_V;
   const uint32_t kd = Bits<K>::DIGITS;
@@ -74,7 +81,7 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   plan_kernel<<<1, 256, 0, stream>>>(pp);
   if (job.marks) cudaEventRecord(job.marks[2], stream);
 
-  auto kern = pass_kernel<K, V, PASS_THREADS, ITEMS, MINB>;
+  auto kern = pass_kernel<K, V, PASS_THREADS, ITEMS, MINB, CLUSTER>;
   static bool attr_set = false;
   if (!attr_set) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -83,6 +90,21 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
     attr_set = true;
   }
   const uint64_t tiles = (job.n + Cfg::TILE - 1) / Cfg::TILE;
+  const uint64_t units = (tiles + CLUSTER - 1) / CLUSTER;  // look-back units (cluster-tiles)
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  lc.gridDim = dim3(unsigned(units * CLUSTER));
+  lc.blockDim = dim3(PASS_THREADS);
+  lc.dynamicSmemBytes = Cfg::DYN_SMEM;
+  lc.stream = stream;
+  if (CLUSTER > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CLUSTER;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+  }
   PassParams pa{};
   pa.keys_in = job.keys_in;
   pa.keys_out = job.keys_out;
@@ -105,7 +127,8 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   for (uint32_t q = 0; q < digits; ++q) {
     pa.pass = q;
     pa.gen = ++(*gen);
-    kern<<<unsigned(tiles), PASS_THREADS, Cfg::DYN_SMEM, stream>>>(pa);
+    e = cudaLaunchKernelEx(&lc, kern, pa);
+    if (e != cudaSuccess) return e;
     if (job.marks) cudaEventRecord(job.marks[3 + q], stream);
   }
   return cudaGetLastError();
@@ -120,6 +143,12 @@ uint32_t radix_tile(int key_bytes, int val_bytes) {
 }
 
 int radix_num_shapes() { return NUM_SHAPES; }
+
+// Measured defaults on GB300 (2^30 uniform keys): 32-bit keys run fastest
+// with 256-thread CTAs of 24 items, four per SM.
+int radix_default_shape(int key_bytes, int val_bytes) {
+  return (val_bytes == 0) ? 1 : 0;
+}
 
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes) {
   const uint64_t t = radix_tile(key_bytes, val_bytes);

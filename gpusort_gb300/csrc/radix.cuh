@@ -20,6 +20,8 @@
 // pipeline is graph-capturable.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "radix_types.cuh"
 
@@ -182,7 +184,28 @@ struct OrderXform {
 // Keys live in the transformed domain between passes: the first pass that
 // runs transforms them on load, the last one restores raw bits on store.
 // Values stay raw and are transformed only to extract a value digit.
-template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS>
+// With CLUSTER > 1, a thread-block cluster of CLUSTER CTAs takes CLUSTER
+// consecutive tiles: the CTAs combine their digit counts through
+// distributed shared memory and only the cluster's first CTA runs the
+// decoupled look-back, over cluster-tiles. Look-back steps per pass drop
+// by CLUSTER, which is what bounds the pass on GB300 (the chain moves a
+// few tiles per L2 round trip).
+// Cluster barrier halves. The warp is reconverged first and the non-.aligned
+// forms are used, because the calls follow divergent code (partial tiles).
+__device__ __forceinline__ void cluster_arrive() {
+  __syncwarp();
+  asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  __syncwarp();
+  asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_sync() {
+  cluster_arrive();
+  cluster_wait();
+}
+
+template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int CLUSTER>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 pass_kernel(PassParams p) {
   using Cfg = PassConfig<K, V, THREADS, ITEMS>;
@@ -197,14 +220,19 @@ pass_kernel(PassParams p) {
   // item row, [63:32] running count. After ranking, [31:0] becomes the
   // digit's start in the tile for that warp. The unstable ranking uses the
   // first RADIX+1 words as tile counters, later tile offsets.
-  __shared__ uint64_t s_tab[WARPS][RADIX + 1];
+  __shared__ __align__(16) uint64_t s_tab[WARPS][RADIX + 1];
   __shared__ uint32_t s_dst_base[RADIX];
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
+  __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
 
   SortPlan& plan = p.work->plan;
   const uint32_t j = plan.exec_index[p.pass];
   if (j == PASS_SKIPPED) return;
+  namespace cg = cooperative_groups;
+  uint32_t crank = 0;
+  if constexpr (CLUSTER > 1) crank = cg::this_cluster().block_rank();
   const uint32_t m = plan.m_exec;
   const bool first = (j == 0);
   const bool last = (j + 1 == m);
@@ -240,17 +268,30 @@ pass_kernel(PassParams p) {
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const OrderXform<VS> vx(p.val_kind, p.desc != 0);
 
-  if (tid == 0) s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
-  {
+  // Tiles (cluster-tiles) are claimed in launch order, so a tile only ever
+  // waits on tiles held by CTAs that are already running.
+  if (tid == 0 && crank == 0) s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
+  if ((smem_addr(&s_tab[0][0]) & 15u) == 0) {
+    static_assert((WARPS * (RADIX + 1)) % 2 == 0, "s_tab is cleared in 16-byte units");
     uint4* z = reinterpret_cast<uint4*>(&s_tab[0][0]);
     constexpr int Z = WARPS * (RADIX + 1) / 2;
     for (int i = tid; i < Z; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
+  } else {  // not expected (the table is declared 16-byte aligned)
+    for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&s_tab[0][0])[i] = 0ull;
+    if (tid == 0) atomicOr(p.err, ERR_SMEM_ALIGN);
   }
-  __syncthreads();
-  const uint32_t tile = s_tile;
+  uint32_t ctile;  // unit of the look-back: a tile, or a cluster-tile
+  if constexpr (CLUSTER > 1) {
+    cluster_sync();
+    ctile = *cg::this_cluster().map_shared_rank(&s_tile, 0);
+  } else {
+    __syncthreads();
+    ctile = s_tile;
+  }
+  const uint32_t tile = ctile * CLUSTER + crank;
   const uint64_t tile_base = uint64_t(tile) * TILE;
-  const uint64_t remaining = n - tile_base;
-  const uint32_t tile_n = remaining < uint64_t(TILE) ? uint32_t(remaining) : uint32_t(TILE);
+  const uint32_t tile_n =
+      tile_base >= n ? 0u : uint32_t(n - tile_base < uint64_t(TILE) ? n - tile_base : uint64_t(TILE));
   const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
 
   // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
@@ -328,10 +369,8 @@ pass_kernel(PassParams p) {
   }
   __syncthreads();
 
-  // Per digit: tile count, per-warp exclusive offsets (stable), aggregate
-  // published at once.
+  // Per digit: tile count, per-warp exclusive offsets (stable).
   uint32_t count = 0;
-  uint64_t* status = p.status + uint64_t(tile) * RADIX;
   if (tid < RADIX) {
     if (unstable) {
       count = s_cnt[tid];
@@ -345,18 +384,38 @@ pass_kernel(PassParams p) {
       }
       count = run;
     }
-    st_relaxed(status + tid, make_status(tile == 0 ? FLAG_INC : FLAG_AGG, p.gen, count));
+    if constexpr (CLUSTER > 1) s_pub[tid] = count;
+  }
+  uint32_t unit_count = count;  // count of the look-back unit
+  uint32_t cl_excl = 0;         // this CTA's offset within the cluster-tile
+  const bool leader = (crank == 0);
+  if constexpr (CLUSTER > 1) {
+    cluster_sync();
+    if (tid < RADIX) {
+      uint32_t total = 0;
+#pragma unroll
+      for (int r = 0; r < CLUSTER; ++r) {
+        const uint32_t c = cg::this_cluster().map_shared_rank(s_pub, r)[tid];
+        if (r < int(crank)) cl_excl += c;
+        total += c;
+      }
+      unit_count = total;
+    }
+  }
+  uint64_t* status = p.status + uint64_t(ctile) * RADIX;
+  if (tid < RADIX && leader) {
+    st_relaxed(status + tid, make_status(ctile == 0 ? FLAG_INC : FLAG_AGG, p.gen, unit_count));
   }
   const uint32_t tile_excl = block_excl_scan_256(count, s_tmp);
 
-  // Decoupled look-back over preceding tiles, LB_WIN words per round,
-  // bounded by spin_limit rounds without progress.
-  if (tid < RADIX) {
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      int64_t t = int64_t(tile) - 1;
+  // Decoupled look-back over preceding units, LB_WIN words per round,
+  // bounded by spin_limit rounds without progress (the cluster's first CTA).
+  uint32_t prefix = 0;
+  if (tid < RADIX && leader) {
+    if (ctile > 0) {
+      int64_t t = int64_t(ctile) - 1;
       uint32_t idle_rounds = 0;
-      const bool stall = p.inject_stall && tile == 1;
+      const bool stall = p.inject_stall && ctile == 1;
       const uint32_t gen = p.gen & GEN_MASK;
       while (true) {
         uint64_t w[LB_WIN];
@@ -384,9 +443,17 @@ pass_kernel(PassParams p) {
           break;
         }
       }
-      st_relaxed(status + tid, make_status(FLAG_INC, p.gen, prefix + count));
+      st_relaxed(status + tid, make_status(FLAG_INC, p.gen, prefix + unit_count));
     }
-    s_dst_base[tid] = plan.binbase[p.pass][tid] + prefix - tile_excl;
+    if constexpr (CLUSTER > 1) s_prefix[tid] = prefix;
+  }
+  if constexpr (CLUSTER > 1) {
+    cluster_sync();
+    if (tid < RADIX) prefix = cg::this_cluster().map_shared_rank(s_prefix, 0)[tid];
+    cluster_arrive();  // the first CTA's s_prefix stays valid until all have read it
+  }
+  if (tid < RADIX) {
+    s_dst_base[tid] = plan.binbase[p.pass][tid] + prefix + cl_excl - tile_excl;
     if (unstable) {
       s_cnt[tid] = tile_excl;
     } else {
@@ -438,6 +505,7 @@ pass_kernel(PassParams p) {
       }
     }
   }
+  if constexpr (CLUSTER > 1) cluster_wait();
 }
 
 }  // namespace gs

@@ -190,7 +190,8 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
 #define GS_DEBUG_SPIN_LIMIT   1
 #define GS_DEBUG_INJECT_STALL 2
 #define GS_DEBUG_BUDGET       3
-#define GS_DEBUG_PASS_SHAPE   4  /* pass-kernel tile shape 0..2 (tuning) */
+#define GS_DEBUG_PASS_SHAPE   4  /* pass-kernel tile shape 0..2 (tuning);
+                                    UINT64_MAX: per-type default */
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
 /* Sort 32-bit keys (GS_U32, GS_I32, GS_F32) in device memory WITHOUT
