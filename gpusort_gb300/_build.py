@@ -68,7 +68,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for obj, log in ex.map(lambda a: _compile(a[0], a[1], extra), jobs):
                 logs.append((obj, log))
-    if jobs or not LIB.exists():
+    stale = not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs)
+    if jobs or stale:
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)

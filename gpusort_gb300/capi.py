@@ -33,6 +33,7 @@ FLAG_DESCENDING = 0x1
 FLAG_PAIRS_STABLE = 0x2
 FLAG_HOST = 0x4
 FLAG_SYNC = 0x8
+FLAG_OFFSETS_HOST = 0x10
 
 ALGO_AUTO, ALGO_RADIX, ALGO_SAMPLE, ALGO_HYK = range(4)
 
@@ -48,6 +49,7 @@ EXPORTED = [
     "gs_last_global_error", "gs_sort_keys", "gs_sort_pairs",
     "gs_segmented_sort_keys", "gs_gather", "gs_phase_times",
     "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set", "gs_sort_keys_noalloc",
+    "gs_segmented_plan_create", "gs_segmented_plan_run", "gs_segmented_plan_destroy",
 ]
 
 _NP_DTYPE = {
@@ -111,6 +113,12 @@ def load() -> C.CDLL:
         L.gs_kernel_times.argtypes = [vp, C.POINTER(C.c_double), i32]
         L.gs_kernel_times.restype = i32
         L.gs_debug_set.argtypes = [vp, i32, u64]
+        L.gs_segmented_plan_create.argtypes = [vp, i32, u64, vp, u32, u32, C.POINTER(vp)]
+        L.gs_segmented_plan_create.restype = i32
+        L.gs_segmented_plan_run.argtypes = [vp, vp, vp, vp]
+        L.gs_segmented_plan_run.restype = i32
+        L.gs_segmented_plan_destroy.argtypes = [vp]
+        L.gs_segmented_plan_destroy.restype = None
         L.gs_sort_keys_noalloc.argtypes = [i32, vp, vp, u64, u32, vp]
         L.gs_sort_keys_noalloc.restype = i32
         for fn in ("gs_ctx_set_stream", "gs_ctx_synchronize", "gs_sort_keys", "gs_sort_pairs",
@@ -222,6 +230,22 @@ class Context:
         code = dtype_code(dtype if dtype is not None else keys_in.dtype)
         return self.L.gs_segmented_sort_keys(self.h, code, _ptr(keys_in), _ptr(keys_out), n,
                                              _ptr(offsets), nseg, f)
+
+    def segmented_plan(self, dtype, n: int, host_offsets: np.ndarray, *, descending=False):
+        """Plan a batched sort (host offsets, nseg+1 entries). Returns a handle."""
+        off = np.ascontiguousarray(host_offsets, dtype=np.uint64)
+        h = C.c_void_p()
+        st = self.L.gs_segmented_plan_create(self.h, dtype_code(dtype), n, off.ctypes.data,
+                                             off.size - 1,
+                                             FLAG_DESCENDING if descending else 0, C.byref(h))
+        self._check(st)
+        return h
+
+    def segmented_run(self, plan, keys_in, keys_out) -> int:
+        return self.L.gs_segmented_plan_run(self.h, plan, _ptr(keys_in), _ptr(keys_out))
+
+    def segmented_destroy(self, plan):
+        self.L.gs_segmented_plan_destroy(plan)
 
     def gather(self, src, dst, perm, elem_bytes, flags=0) -> int:
         n = _count(perm)

@@ -4,10 +4,12 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/gpusort_gb300.h"
 #include "engine.h"
 #include "common.cuh"
+#include "radix_types.cuh"
 
 namespace {
 
@@ -123,15 +125,11 @@ void phase_mark(gs_ctx* ctx, const char* name) {
 
 // Bring the look-back status words to the size a job needs and keep the
 // generation tags unambiguous.
+// (Look-back tags are drawn on the device from work->gen_counter; a tag
+// repeats only after 2^30 passes.)
 gs_status prepare_status(gs_ctx* ctx, size_t words, uint32_t passes) {
-  gs_status st = ensure(ctx, ctx->status, words * sizeof(uint64_t), true);
-  if (st != GS_OK) return st;
-  if (ctx->gen + passes + 1 >= gs::GEN_MASK) {
-    cudaError_t e = cudaMemsetAsync(ctx->status.ptr, 0, ctx->status.bytes, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(status)");
-    ctx->gen = 0;
-  }
-  return GS_OK;
+  (void)passes;
+  return ensure(ctx, ctx->status, words * sizeof(uint64_t), true);
 }
 
 gs_status check_err_word(gs_ctx* ctx) {
@@ -330,6 +328,7 @@ gs_ctx* gs_ctx_create(int device, uint64_t hbm_budget_bytes) {
   }
   ctx->held += gs::sort_work_bytes() + 256;
   cudaMemsetAsync(ctx->err, 0, 256, ctx->stream);
+  cudaMemsetAsync(ctx->work, 0, gs::sort_work_bytes(), ctx->stream);
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
   for (auto& ev : ctx->kev) cudaEventCreate(&ev);
   cudaStreamSynchronize(ctx->stream);
@@ -377,11 +376,107 @@ gs_status gs_sort_pairs(gs_ctx* ctx, gs_dtype key_dtype, gs_dtype val_dtype, con
                      opts);
 }
 
+gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
+                                   const uint64_t* host_offsets, uint32_t nseg, uint32_t flags,
+                                   gs_seg_plan** plan) {
+  if (!ctx || !plan) return fail(ctx, GS_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *plan = nullptr;
+  int kb = 0;
+  uint32_t kk = 0;
+  if (!dtype_info(dtype, &kb, &kk)) return fail(ctx, GS_ERR_BAD_DTYPE, "unknown key dtype");
+  if (n > MAX_N) return fail(ctx, GS_ERR_TOO_LARGE, "n exceeds 2^32-1 elements");
+  if (!host_offsets) return fail(ctx, GS_ERR_INVALID, "null offsets");
+  cudaSetDevice(ctx->props.device);
+  gs_seg_plan* pl = gs::seg_plan_new();
+  const std::string err = gs::seg_plan_build(pl, host_offsets, nseg, n, kb, kk,
+                                             (flags & GS_FLAG_DESCENDING) != 0,
+                                             gs::radix_segmented_shape(kb));
+  if (!err.empty()) {
+    gs::seg_plan_free(pl);
+    return fail(ctx, err.find("allocation") != std::string::npos ? GS_ERR_OOM : GS_ERR_INVALID,
+                err);
+  }
+  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st == GS_OK)
+    st = prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX,
+                        uint32_t(kb));
+  if (st != GS_OK) {
+    gs::seg_plan_free(pl);
+    return st;
+  }
+  cudaStreamSynchronize(ctx->stream);
+  *plan = pl;
+  return GS_OK;
+}
+
+gs_status gs_segmented_plan_run(gs_ctx* ctx, const gs_seg_plan* plan, const void* in, void* out) {
+  if (!ctx || !plan) return fail(ctx, GS_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (gs::seg_plan_n(plan) == 0) return GS_OK;
+  if (!in || !out) return fail(ctx, GS_ERR_INVALID, "null data pointer");
+  if (ctx->alt_k.bytes < gs::seg_plan_n(plan) * gs::seg_plan_key_bytes(plan))
+    return fail(ctx, GS_ERR_INVALID, "context scratch was not sized for this plan");
+  cudaError_t e = gs::seg_plan_run(plan, in, out, ctx->alt_k.ptr,
+                                   static_cast<uint64_t*>(ctx->status.ptr),
+                                   &ctx->work->gen_counter, ctx->err, ctx->spin_limit,
+                                   ctx->props, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "segmented sort launch");
+  return GS_OK;
+}
+
+void gs_segmented_plan_destroy(gs_seg_plan* plan) {
+  if (plan) gs::seg_plan_free(plan);
+}
+
 gs_status gs_segmented_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in, void* out,
                                  uint64_t n, const uint64_t* offsets, uint32_t nseg,
                                  uint32_t flags) {
-  (void)dtype; (void)in; (void)out; (void)n; (void)offsets; (void)nseg; (void)flags;
-  return fail(ctx, GS_ERR_INVALID, "segmented sort is not available in this build");
+  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
+  int kb = 0;
+  uint32_t kk = 0;
+  if (!dtype_info(dtype, &kb, &kk)) return fail(ctx, GS_ERR_BAD_DTYPE, "unknown key dtype");
+  if (!offsets) return fail(ctx, GS_ERR_INVALID, "null offsets");
+  if (n == 0) return GS_OK;
+  if (!in || !out) return fail(ctx, GS_ERR_INVALID, "null data pointer");
+  std::vector<uint64_t> host_off;
+  const uint64_t* hoff = offsets;
+  if (!(flags & GS_FLAG_OFFSETS_HOST)) {
+    host_off.resize(size_t(nseg) + 1);
+    cudaSetDevice(ctx->props.device);
+    cudaError_t e = cudaMemcpy(host_off.data(), offsets, host_off.size() * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "offsets copy");
+    hoff = host_off.data();
+  }
+  gs_seg_plan* plan = nullptr;
+  gs_status st = gs_segmented_plan_create(ctx, dtype, n, hoff, nseg, flags, &plan);
+  if (st != GS_OK) return st;
+  const void* din = in;
+  void* dout = out;
+  if (flags & GS_FLAG_HOST) {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    st = ensure(ctx, ctx->stage_k, size_t(n) * kb);
+    if (st == GS_OK) {
+      cudaError_t e = cudaMemcpyAsync(ctx->stage_k.ptr, in, size_t(n) * kb,
+                                      cudaMemcpyHostToDevice, ctx->stream);
+      if (e != cudaSuccess) st = cuda_fail(ctx, e, "host to device copy");
+    }
+    din = dout = ctx->stage_k.ptr;
+  }
+  if (st == GS_OK) st = gs_segmented_plan_run(ctx, plan, din, dout);
+  if (st == GS_OK && (flags & GS_FLAG_HOST)) {
+    cudaError_t e = cudaMemcpyAsync(out, ctx->stage_k.ptr, size_t(n) * kb,
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) st = cuda_fail(ctx, e, "device to host copy");
+  }
+  if (st == GS_OK) {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    st = check_err_word(ctx);
+  } else {
+    cudaStreamSynchronize(ctx->stream);
+  }
+  gs_segmented_plan_destroy(plan);
+  return st;
 }
 
 gs_status gs_gather(gs_ctx* ctx, const void* in, void* out, uint64_t n, uint32_t elem_bytes,

@@ -44,6 +44,7 @@ struct RadixJob {
   // each pass q (3 + q). Needs 3 + digits events.
   cudaEvent_t* marks = nullptr;
   int shape = 0;                    // pass-kernel tile shape (0 .. radix_num_shapes()-1)
+  uint32_t* gen_counter = nullptr;  // look-back tag counter of `status` (default: in work)
 };
 
 // Smallest tile (elements) of the pass kernel over all shapes: sizes the
@@ -56,6 +57,36 @@ size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
 size_t sort_work_bytes();
+
+// Large segments of a batched sort, for the segmented form of the passes.
+struct SegJob {
+  const uint32_t* tile_start;  // nseg + 1 first-tile indexes
+  const uint64_t* range;       // nseg (begin, end) element pairs
+  const uint32_t* binbase;     // [nseg][digits][256]
+  uint32_t nseg;
+  uint32_t digits;
+  uint32_t total_tiles;
+};
+uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape);
+int radix_segmented_shape(int key_bytes);
+// Enqueue only the digit passes over the large segments (plan and bin
+// bases already prepared in job.work / sj.binbase).
+cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const DeviceProps& props,
+                                uint32_t* gen, cudaStream_t stream);
+
+}  // namespace gs
+struct gs_seg_plan;
+namespace gs {
+std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, uint64_t n,
+                           int key_bytes, uint32_t kind, bool desc, int shape);
+void seg_plan_free(gs_seg_plan* pl);
+gs_seg_plan* seg_plan_new();
+uint32_t seg_plan_large_tiles(const gs_seg_plan* pl);
+uint64_t seg_plan_n(const gs_seg_plan* pl);
+int seg_plan_key_bytes(const gs_seg_plan* pl);
+cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void* alt,
+                         uint64_t* status, uint32_t* gen_counter, uint32_t* err,
+                         uint32_t spin_limit, const DeviceProps& props, cudaStream_t st);
 
 // Set the message gs_last_global_error() returns on this thread.
 void set_last_global_error(const std::string& msg);

@@ -58,7 +58,7 @@ void setup(int dev, DeviceSlot& s) {
   s.setup_err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (s.setup_err != cudaSuccess) return;
   s.scratch = static_cast<unsigned char*>(p);
-  s.setup_err = cudaMemset(s.scratch + kAltBytes, 0, kStatusBytes);
+  s.setup_err = cudaMemset(s.scratch + kAltBytes, 0, kStatusBytes + kWorkBytes);
   if (s.setup_err != cudaSuccess) return;
   s.props.device = dev;
   cudaDeviceGetAttribute(&s.props.num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -111,14 +111,8 @@ gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out, uint64
   job.key_bytes = 4;
   job.key_kind = kind;
   job.desc = (flags & GS_FLAG_DESCENDING) != 0;
-  // Generation tags: each call takes its own range; when the tags wrap, the
-  // look-back words are cleared again.
-  uint32_t gen = s.gen.fetch_add(8);
-  if (gen + 8 >= gs::GEN_MASK) {
-    cudaMemsetAsync(job.status, 0, kStatusBytes, st);
-    s.gen.store(8);
-    gen = 0;
-  }
+  // Look-back tags are drawn on the device from the work area's counter.
+  uint32_t gen = 0;
   cudaError_t e = cudaMemsetAsync(job.err, 0, sizeof(uint32_t), st);
   if (e == cudaSuccess) e = gs::launch_radix_sort(job, s.props, &gen, st);
   if (e != cudaSuccess) return fail(GS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

@@ -4,6 +4,54 @@
 
 namespace gs {
 
+// ---------------------------------------------------------------------------
+// Plan: bin bases, skipped digits, pass numbering. One block of 256 threads.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) plan_kernel(PlanParams p) {
+  __shared__ uint32_t s_tmp[8];
+  __shared__ uint32_t s_trivial[MAX_DIGITS];
+  SortPlan& plan = p.work->plan;
+  const uint32_t tid = threadIdx.x;
+  if (tid < MAX_DIGITS) s_trivial[tid] = 0;
+  __syncthreads();
+  for (uint32_t q = 0; q < p.digits; ++q) {
+    const uint32_t c = p.work->hist[q][tid];
+    if (uint64_t(c) == p.n) s_trivial[q] = 1;  // one bin holds every key
+    const uint32_t ex = block_excl_scan_256(c, s_tmp);
+    plan.binbase[q][tid] = ex;
+  }
+  if (tid < MAX_DIGITS) plan.tile_counter[tid] = 0;
+  // Look-back tags come from the device, so a replayed CUDA graph never
+  // meets its own earlier words with a matching tag.
+  if (tid == 0) plan.gen_base = atomicAdd(p.gen_counter, uint32_t(MAX_DIGITS + 1));
+  __syncthreads();
+  if (tid == 0) {
+    bool exec[MAX_DIGITS];
+    uint32_t m = 0;
+    for (uint32_t q = 0; q < MAX_DIGITS; ++q) {
+      exec[q] = (q < p.digits) && !s_trivial[q];
+      m += exec[q];
+    }
+    // Every key equal: nothing to reorder, but a copy (or the reversal of a
+    // stable descending pair sort) still has to reach the output.
+    if (m == 0 && (!p.in_place || p.reverse_first)) {
+      exec[p.digits - 1] = true;
+      m = 1;
+    }
+    // In place, the first pass may not write its own input: make the pass
+    // count even so the first pass writes the scratch buffer.
+    if (p.in_place && (m & 1u)) {
+      for (uint32_t q = 0; q < p.digits; ++q) {
+        if (!exec[q]) { exec[q] = true; ++m; break; }
+      }
+    }
+    uint32_t j = 0;
+    for (uint32_t q = 0; q < MAX_DIGITS; ++q) plan.exec_index[q] = exec[q] ? j++ : PASS_SKIPPED;
+    plan.m_exec = m;
+  }
+}
+
+
 namespace {
 
 constexpr int UPSWEEP_THREADS = 512;
@@ -35,52 +83,18 @@ struct PassShape : Shape<(S == 0 ? 512 : 256), 8, (S == 0 ? 2 : 4), 1> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 256 * 8;  // smallest tile of any shape
 
+// Enqueue the digit passes (plan already in job.work). With `sj` the passes
+// sort the large segments of a batch; the shape must then run without
+// clusters.
 template <typename K, typename V, int S>
-cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
-                cudaStream_t stream) {
+cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits, uint32_t vd,
+                          const DeviceProps& props, uint32_t* gen, cudaStream_t stream) {
   constexpr int PASS_THREADS = PassShape<K, V, S>::THREADS;
   constexpr int ITEMS = PassShape<K, V, S>::ITEMS;
   constexpr int MINB = PassShape<K, V, S>::MINB;
   constexpr int CLUSTER = PassShape<K, V, S>::CLUSTER;
   using Cfg = PassConfig<K, V, PASS_THREADS, ITEMS>;
-  constexpr bool HAS_V = Cfg::HAS_V;
-  const uint32_t kd = Bits<K>::DIGITS;
-  uint32_t vd = 0;
-  if constexpr (HAS_V) vd = job.ties_by_value ? Bits<V>::DIGITS : 0;
-  const uint32_t digits = kd + vd;
-
-  if (job.marks) cudaEventRecord(job.marks[0], stream);
-  cudaError_t e = cudaMemsetAsync(job.work, 0, sizeof(uint32_t) * MAX_DIGITS * RADIX, stream);
-  if (e != cudaSuccess) return e;
-
-  UpsweepParams up{};
-  up.keys = job.keys_in;
-  up.vals = job.vals_in;
-  up.n = job.n;
-  up.key_kind = job.key_kind;
-  up.val_kind = job.val_kind;
-  up.desc = job.desc;
-  up.val_digits = vd;
-  up.work = job.work;
-  const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
-  uint64_t ublocks = (job.n + chunk - 1) / chunk;
-  const uint64_t umax = uint64_t(props.num_sms) * 4;
-  if (ublocks > umax) ublocks = umax;
-  if (ublocks == 0) ublocks = 1;
-  upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL>
-      <<<unsigned(ublocks), UPSWEEP_THREADS, 0, stream>>>(up);
-  if (job.marks) cudaEventRecord(job.marks[1], stream);
-
-  PlanParams pp{};
-  pp.work = job.work;
-  pp.n = job.n;
-  pp.digits = digits;
-  pp.in_place = (job.keys_in == job.keys_out) ||
-                (HAS_V && job.vals_in == job.vals_out);
-  pp.reverse_first = job.reverse_first;
-  plan_kernel<<<1, 256, 0, stream>>>(pp);
-  if (job.marks) cudaEventRecord(job.marks[2], stream);
-
+  cudaError_t e = cudaSuccess;
   auto kern = pass_kernel<K, V, PASS_THREADS, ITEMS, MINB, CLUSTER>;
   static bool attr_set = false;
   if (!attr_set) {
@@ -89,7 +103,8 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  const uint64_t tiles = (job.n + Cfg::TILE - 1) / Cfg::TILE;
+  if (sj != nullptr && CLUSTER > 1) return cudaErrorInvalidValue;
+  const uint64_t tiles = sj != nullptr ? sj->total_tiles : (job.n + Cfg::TILE - 1) / Cfg::TILE;
   const uint64_t units = (tiles + CLUSTER - 1) / CLUSTER;  // look-back units (cluster-tiles)
   cudaLaunchConfig_t lc = {};
   cudaLaunchAttribute attr[1];
@@ -124,9 +139,17 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   pa.inject_stall = job.inject_stall;
   pa.work = job.work;
   pa.err = job.err;
+  if (sj != nullptr) {
+    pa.seg_tile_start = sj->tile_start;
+    pa.seg_range = sj->range;
+    pa.seg_binbase = sj->binbase;
+    pa.nseg = sj->nseg;
+    pa.seg_digits = sj->digits;
+  }
+  if (tiles == 0) return cudaSuccess;
+  (void)gen;
   for (uint32_t q = 0; q < digits; ++q) {
     pa.pass = q;
-    pa.gen = ++(*gen);
     e = cudaLaunchKernelEx(&lc, kern, pa);
     if (e != cudaSuccess) return e;
     if (job.marks) cudaEventRecord(job.marks[3 + q], stream);
@@ -134,7 +157,88 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   return cudaGetLastError();
 }
 
+template <typename K, typename V, int S>
+cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
+                cudaStream_t stream) {
+  constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
+  const uint32_t kd = Bits<K>::DIGITS;
+  uint32_t vd = 0;
+  if constexpr (HAS_V) vd = job.ties_by_value ? Bits<V>::DIGITS : 0;
+  const uint32_t digits = kd + vd;
+
+  if (job.marks) cudaEventRecord(job.marks[0], stream);
+  cudaError_t e = cudaMemsetAsync(job.work, 0, sizeof(uint32_t) * MAX_DIGITS * RADIX, stream);
+  if (e != cudaSuccess) return e;
+
+  UpsweepParams up{};
+  up.keys = job.keys_in;
+  up.vals = job.vals_in;
+  up.n = job.n;
+  up.key_kind = job.key_kind;
+  up.val_kind = job.val_kind;
+  up.desc = job.desc;
+  up.val_digits = vd;
+  up.work = job.work;
+  const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
+  uint64_t ublocks = (job.n + chunk - 1) / chunk;
+  const uint64_t umax = uint64_t(props.num_sms) * 4;
+  if (ublocks > umax) ublocks = umax;
+  if (ublocks == 0) ublocks = 1;
+  upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL>
+      <<<unsigned(ublocks), UPSWEEP_THREADS, 0, stream>>>(up);
+  if (job.marks) cudaEventRecord(job.marks[1], stream);
+
+  PlanParams pp{};
+  pp.work = job.work;
+  pp.n = job.n;
+  pp.digits = digits;
+  pp.in_place = (job.keys_in == job.keys_out) ||
+                (HAS_V && job.vals_in == job.vals_out);
+  pp.reverse_first = job.reverse_first;
+  pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
+  plan_kernel<<<1, 256, 0, stream>>>(pp);
+  if (job.marks) cudaEventRecord(job.marks[2], stream);
+  return launch_passes<K, V, S>(job, nullptr, digits, vd, props, gen, stream);
+}
+
 }  // namespace
+
+template <typename K, typename V>
+uint32_t shape_tile(int shape) {
+  switch (shape) {
+    case 1: return PassShape<K, V, 1>::THREADS * PassShape<K, V, 1>::ITEMS;
+    case 2: return PassShape<K, V, 2>::THREADS * PassShape<K, V, 2>::ITEMS;
+    default: return PassShape<K, V, 0>::THREADS * PassShape<K, V, 0>::ITEMS;
+  }
+}
+
+uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape) {
+  if (val_bytes != 0) return 0;  // segmented sorts are keys only
+  return key_bytes == 4 ? shape_tile<uint32_t, NoValue>(shape) : shape_tile<uint64_t, NoValue>(shape);
+}
+
+int radix_segmented_shape(int key_bytes) {
+  // Non-cluster shape with the measured best tile for the key width.
+  (void)key_bytes;
+  return 1;
+}
+
+cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const DeviceProps& props,
+                                uint32_t* gen, cudaStream_t stream) {
+  const uint32_t digits = sj.digits;
+  if (job.key_bytes == 4) {
+    switch (job.shape) {
+      case 0: return launch_passes<uint32_t, NoValue, 0>(job, &sj, digits, 0, props, gen, stream);
+      case 1: return launch_passes<uint32_t, NoValue, 1>(job, &sj, digits, 0, props, gen, stream);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  switch (job.shape) {
+    case 0: return launch_passes<uint64_t, NoValue, 0>(job, &sj, digits, 0, props, gen, stream);
+    case 1: return launch_passes<uint64_t, NoValue, 1>(job, &sj, digits, 0, props, gen, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 uint32_t radix_tile(int key_bytes, int val_bytes) {
   (void)key_bytes;

@@ -101,50 +101,6 @@ upsweep_kernel(UpsweepParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// Plan: bin bases, skipped digits, pass numbering. One block of 256 threads.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) plan_kernel(PlanParams p) {
-  __shared__ uint32_t s_tmp[8];
-  __shared__ uint32_t s_trivial[MAX_DIGITS];
-  SortPlan& plan = p.work->plan;
-  const uint32_t tid = threadIdx.x;
-  if (tid < MAX_DIGITS) s_trivial[tid] = 0;
-  __syncthreads();
-  for (uint32_t q = 0; q < p.digits; ++q) {
-    const uint32_t c = p.work->hist[q][tid];
-    if (uint64_t(c) == p.n) s_trivial[q] = 1;  // one bin holds every key
-    const uint32_t ex = block_excl_scan_256(c, s_tmp);
-    plan.binbase[q][tid] = ex;
-  }
-  if (tid < MAX_DIGITS) plan.tile_counter[tid] = 0;
-  __syncthreads();
-  if (tid == 0) {
-    bool exec[MAX_DIGITS];
-    uint32_t m = 0;
-    for (uint32_t q = 0; q < MAX_DIGITS; ++q) {
-      exec[q] = (q < p.digits) && !s_trivial[q];
-      m += exec[q];
-    }
-    // Every key equal: nothing to reorder, but a copy (or the reversal of a
-    // stable descending pair sort) still has to reach the output.
-    if (m == 0 && (!p.in_place || p.reverse_first)) {
-      exec[p.digits - 1] = true;
-      m = 1;
-    }
-    // In place, the first pass may not write its own input: make the pass
-    // count even so the first pass writes the scratch buffer.
-    if (p.in_place && (m & 1u)) {
-      for (uint32_t q = 0; q < p.digits; ++q) {
-        if (!exec[q]) { exec[q] = true; ++m; break; }
-      }
-    }
-    uint32_t j = 0;
-    for (uint32_t q = 0; q < MAX_DIGITS; ++q) plan.exec_index[q] = exec[q] ? j++ : PASS_SKIPPED;
-    plan.m_exec = m;
-  }
-}
-
-// ---------------------------------------------------------------------------
 // One onesweep pass.
 // ---------------------------------------------------------------------------
 template <typename K, typename V, int THREADS, int ITEMS>
@@ -224,6 +180,7 @@ pass_kernel(PassParams p) {
   __shared__ uint32_t s_dst_base[RADIX];
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_seg;
   __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
   __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
 
@@ -234,6 +191,7 @@ pass_kernel(PassParams p) {
   uint32_t crank = 0;
   if constexpr (CLUSTER > 1) crank = cg::this_cluster().block_rank();
   const uint32_t m = plan.m_exec;
+  const uint32_t gen = (plan.gen_base + p.pass + 1) & GEN_MASK;  // this pass's look-back tag
   const bool first = (j == 0);
   const bool last = (j + 1 == m);
 
@@ -289,9 +247,28 @@ pass_kernel(PassParams p) {
     ctile = s_tile;
   }
   const uint32_t tile = ctile * CLUSTER + crank;
-  const uint64_t tile_base = uint64_t(tile) * TILE;
+  // Batched sorts (CLUSTER == 1): the tile's segment, its element range and
+  // its first tile, where the segment's look-back chain starts.
+  uint32_t seg = 0, first_unit = 0;
+  uint64_t e0 = 0, e1 = n;
+  if (p.seg_tile_start != nullptr) {
+    if (tid == 0) {
+      uint32_t lo = 0, hi = p.nseg;  // last s with seg_tile_start[s] <= tile
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (p.seg_tile_start[mid] <= tile) lo = mid; else hi = mid;
+      }
+      s_seg = lo;
+    }
+    __syncthreads();
+    seg = s_seg;
+    first_unit = p.seg_tile_start[seg];
+    e0 = p.seg_range[2 * seg];
+    e1 = p.seg_range[2 * seg + 1];
+  }
+  const uint64_t tile_base = e0 + uint64_t(tile - first_unit) * TILE;
   const uint32_t tile_n =
-      tile_base >= n ? 0u : uint32_t(n - tile_base < uint64_t(TILE) ? n - tile_base : uint64_t(TILE));
+      tile_base >= e1 ? 0u : uint32_t(e1 - tile_base < uint64_t(TILE) ? e1 - tile_base : uint64_t(TILE));
   const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
 
   // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
@@ -404,7 +381,8 @@ pass_kernel(PassParams p) {
   }
   uint64_t* status = p.status + uint64_t(ctile) * RADIX;
   if (tid < RADIX && leader) {
-    st_relaxed(status + tid, make_status(ctile == 0 ? FLAG_INC : FLAG_AGG, p.gen, unit_count));
+    st_relaxed(status + tid,
+               make_status(ctile == first_unit ? FLAG_INC : FLAG_AGG, gen, unit_count));
   }
   const uint32_t tile_excl = block_excl_scan_256(count, s_tmp);
 
@@ -412,11 +390,10 @@ pass_kernel(PassParams p) {
   // bounded by spin_limit rounds without progress (the cluster's first CTA).
   uint32_t prefix = 0;
   if (tid < RADIX && leader) {
-    if (ctile > 0) {
+    if (ctile > first_unit) {
       int64_t t = int64_t(ctile) - 1;
       uint32_t idle_rounds = 0;
       const bool stall = p.inject_stall && ctile == 1;
-      const uint32_t gen = p.gen & GEN_MASK;
       while (true) {
         uint64_t w[LB_WIN];
 #pragma unroll
@@ -443,7 +420,7 @@ pass_kernel(PassParams p) {
           break;
         }
       }
-      st_relaxed(status + tid, make_status(FLAG_INC, p.gen, prefix + unit_count));
+      st_relaxed(status + tid, make_status(FLAG_INC, gen, prefix + unit_count));
     }
     if constexpr (CLUSTER > 1) s_prefix[tid] = prefix;
   }
@@ -453,7 +430,10 @@ pass_kernel(PassParams p) {
     cluster_arrive();  // the first CTA's s_prefix stays valid until all have read it
   }
   if (tid < RADIX) {
-    s_dst_base[tid] = plan.binbase[p.pass][tid] + prefix + cl_excl - tile_excl;
+    const uint32_t bb = p.seg_binbase != nullptr
+                            ? p.seg_binbase[(size_t(seg) * p.seg_digits + p.pass) * RADIX + tid]
+                            : plan.binbase[p.pass][tid];
+    s_dst_base[tid] = uint32_t(e0) + bb + prefix + cl_excl - tile_excl;
     if (unstable) {
       s_cnt[tid] = tile_excl;
     } else {
@@ -481,7 +461,7 @@ pass_kernel(PassParams p) {
 
   // Scatter: consecutive tile positions of one digit go to consecutive
   // output addresses.
-  const uint32_t n32 = uint32_t(n);  // n < 2^32
+  const uint32_t n32 = uint32_t(e1);  // end of the segment (n < 2^32)
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     const uint32_t r = uint32_t(i) * THREADS + tid;

@@ -7,6 +7,7 @@
 namespace gs {
 
 struct SortPlan {
+  uint32_t gen_base;                      // look-back tag of this sort (pass q: +q+1)
   uint32_t m_exec;                        // passes that run
   uint32_t exec_index[MAX_DIGITS];        // 0..m_exec-1, or PASS_SKIPPED
   uint32_t tile_counter[MAX_DIGITS];      // tile claim counters per pass
@@ -17,6 +18,7 @@ struct SortPlan {
 struct SortWork {
   uint32_t hist[MAX_DIGITS][RADIX];
   SortPlan plan;
+  uint32_t gen_counter;  // per status buffer: the next free look-back tag
 };
 
 struct UpsweepParams {
@@ -31,6 +33,7 @@ struct UpsweepParams {
 
 struct PlanParams {
   SortWork* work;
+  uint32_t* gen_counter;  // shared by every sort that uses the same status words
   uint64_t n;
   uint32_t digits;        // val_digits + key_digits
   uint32_t in_place;      // an output aliases its input
@@ -52,11 +55,20 @@ struct PassParams {
   uint32_t reverse_first;
   uint32_t first_unstable;  // the first pass that runs may rank unstably
   uint64_t* status;       // num_tiles * RADIX look-back words
-  uint32_t gen;
   uint32_t spin_limit;
   uint32_t inject_stall;  // test hook: tile 1 waits on a flag nobody sets
   SortWork* work;
   uint32_t* err;
+  // Batched (segmented) sorts: when seg_tile_start is set, tiles of
+  // segment s are [seg_tile_start[s], seg_tile_start[s+1]), its elements
+  // [seg_range[2s], seg_range[2s+1]), and its bin bases are
+  // seg_binbase[(s * seg_digits + pass) * RADIX + digit]. Each segment's
+  // first tile starts its own look-back chain.
+  const uint32_t* seg_tile_start;
+  const uint64_t* seg_range;
+  const uint32_t* seg_binbase;
+  uint32_t nseg;
+  uint32_t seg_digits;
 };
 
 }  // namespace gs

@@ -1,0 +1,405 @@
+// Batched sorting of many independent segments (gs_segmented_sort_keys and
+// the plan/run pair used for CUDA-graph capture).
+//
+// Each segment is sorted on its own, as one rank's local sort of the
+// reference would be (include/omp/omp_utils.h:147-207). Two kernels share
+// the work:
+// * group_sort_kernel: segments of at most GROUP_KEYS keys are packed, in
+//   order, into groups of consecutive segments; one CTA loads a group into
+//   shared memory and radix-sorts it by (local segment id, key) - an LSD
+//   sort over the key's digits and then the segment id - and writes it back
+//   in place of the group;
+// * the onesweep pass kernel (radix.cuh) in its segmented form for larger
+//   segments: tiles never straddle segments, each segment has its own bin
+//   bases, and each segment's first tile starts its own look-back chain.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gpusort_gb300.h"
+#include "engine.h"
+#include "radix.cuh"
+
+namespace gs {
+
+constexpr int GROUP_THREADS = 256;
+constexpr int GROUP_ITEMS = 16;
+constexpr uint32_t GROUP_KEYS = GROUP_THREADS * GROUP_ITEMS;  // 4096
+constexpr uint32_t GROUP_MAX_SEGS = 256;                     // segment id is one digit
+
+struct SegGroup {
+  uint64_t start;      // first element of the group
+  uint32_t count;      // elements in the group (<= GROUP_KEYS)
+  uint32_t first_seg;  // index of its first segment in seg_starts_rel
+  uint32_t nsegs;      // segments in the group (<= GROUP_MAX_SEGS)
+  uint32_t pad;
+};
+
+struct GroupSortParams {
+  const void* in;
+  void* out;
+  const SegGroup* groups;
+  const uint32_t* seg_starts_rel;  // per group: nsegs + 1 offsets relative to start
+  uint32_t key_kind;
+  uint32_t desc;
+};
+
+// One CTA sorts one group in shared memory: LSD passes over the key's
+// digits (stable ranking with shared peer masks, as in the pass kernel;
+// the first pass may be unstable), then one pass over the local segment id
+// when the group holds several segments.
+template <typename K>
+__global__ void __launch_bounds__(GROUP_THREADS)
+group_sort_kernel(GroupSortParams p) {
+  constexpr int THREADS = GROUP_THREADS;
+  constexpr int ITEMS = GROUP_ITEMS;
+  constexpr int WARPS = THREADS / 32;
+  constexpr int TILE = GROUP_KEYS;
+  // Dynamic: two key buffers, then two segment-id buffers.
+  extern __shared__ __align__(16) uint8_t s_dyn[];
+  K* s_key[2] = {reinterpret_cast<K*>(s_dyn), reinterpret_cast<K*>(s_dyn) + TILE};
+  uint16_t* s_sid[2] = {reinterpret_cast<uint16_t*>(s_dyn + 2 * TILE * sizeof(K)),
+                        reinterpret_cast<uint16_t*>(s_dyn + 2 * TILE * sizeof(K)) + TILE};
+  __shared__ __align__(16) uint64_t s_tab[WARPS][RADIX + 1];
+  __shared__ uint32_t s_sstart[GROUP_MAX_SEGS + 1];
+  __shared__ uint32_t s_tmp[8];
+
+  const SegGroup g = p.groups[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const OrderXform<K> kx(p.key_kind, p.desc != 0);
+  const K* in = static_cast<const K*>(p.in) + g.start;
+  K* out = static_cast<K*>(p.out) + g.start;
+  const uint32_t cnt = g.count;
+  for (uint32_t i = tid; i <= g.nsegs; i += THREADS) s_sstart[i] = p.seg_starts_rel[g.first_seg + i];
+  __syncthreads();
+  // Load (transformed) keys and local segment ids.
+  for (uint32_t i = tid; i < cnt; i += THREADS) {
+    s_key[0][i] = kx.fwd(in[i]);
+    uint32_t lo = 0, hi = g.nsegs;  // last s with s_sstart[s] <= i
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s_sstart[mid] <= i) lo = mid; else hi = mid;
+    }
+    s_sid[0][i] = uint16_t(lo);
+  }
+  const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;
+  const uint32_t lt = lanemask_lt();
+  const int key_digits = int(sizeof(K));
+  const int passes = key_digits + (g.nsegs > 1 ? 1 : 0);
+  int cur = 0;
+  for (int q = 0; q < passes; ++q) {
+    const bool sid_pass = q == key_digits;
+    const uint32_t shift = RADIX_BITS * uint32_t(q);
+    for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&s_tab[0][0])[i] = 0ull;
+    __syncthreads();
+    K keys[ITEMS];
+    uint32_t rank2[ITEMS / 2];
+#pragma unroll
+    for (int i = 0; i < ITEMS / 2; ++i) rank2[i] = 0;
+    auto digit_at = [&](int i) -> uint32_t {
+      return sid_pass ? uint32_t(s_sid[cur][wloc + 32 * i])
+                      : (uint32_t(keys[i] >> shift) & (RADIX - 1));
+    };
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const uint32_t l = wloc + 32 * i;
+      keys[i] = l < cnt ? s_key[cur][l] : K(0);
+    }
+    uint64_t* tab = s_tab[warp];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const uint32_t d = (wloc + 32 * i < cnt) ? digit_at(i) : uint32_t(RADIX);
+      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]), 1u << lane);
+      __syncwarp();
+      const uint64_t e = tab[d];
+      __syncwarp();
+      const uint32_t peers = uint32_t(e), below = peers & lt, base = uint32_t(e >> 32);
+      rank2[i >> 1] |= (base + __popc(below)) << (16 * (i & 1));
+      if (below == 0) tab[d] = uint64_t(base + __popc(peers)) << 32;
+      __syncwarp();
+    }
+    __syncthreads();
+    uint32_t count = 0;
+    if (tid < RADIX) {
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = uint32_t(s_tab[w][tid] >> 32);
+        s_tab[w][tid] = run;
+        run += c;
+      }
+      count = run;
+    }
+    const uint32_t excl = block_excl_scan_256(count, s_tmp);
+    if (tid < RADIX) {
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) s_tab[w][tid] += excl;
+    }
+    __syncthreads();
+    const uint32_t* off = reinterpret_cast<const uint32_t*>(&s_tab[warp][0]);
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const uint32_t l = wloc + 32 * i;
+      if (l < cnt) {
+        const uint32_t pos = off[2 * digit_at(i)] + ((rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu);
+        s_key[cur ^ 1][pos] = keys[i];
+        s_sid[cur ^ 1][pos] = s_sid[cur][l];
+      }
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  for (uint32_t i = tid; i < cnt; i += THREADS) out[i] = kx.inv(s_key[cur][i]);
+}
+
+template <typename K>
+constexpr size_t group_sort_dyn_smem() {
+  return 2 * size_t(GROUP_KEYS) * (sizeof(K) + sizeof(uint16_t));
+}
+
+// Histograms of every digit, per large segment.
+struct SegHistParams {
+  const void* keys;
+  const uint32_t* seg_tile_start;
+  const uint64_t* seg_range;
+  uint32_t nseg;
+  uint32_t tile;        // elements per tile (the pass kernel's)
+  uint32_t total_tiles;
+  uint32_t key_kind;
+  uint32_t desc;
+  uint32_t* hist;       // [nseg][digits][RADIX]
+};
+
+template <typename K>
+__global__ void __launch_bounds__(256) seg_hist_kernel(SegHistParams p) {
+  constexpr int KD = Bits<K>::DIGITS;
+  __shared__ uint32_t s_h[KD * RADIX];
+  __shared__ uint32_t s_seg;
+  const OrderXform<K> kx(p.key_kind, p.desc != 0);
+  const K* keys = static_cast<const K*>(p.keys);
+  for (uint32_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+    for (int i = threadIdx.x; i < KD * RADIX; i += blockDim.x) s_h[i] = 0;
+    if (threadIdx.x == 0) {
+      uint32_t lo = 0, hi = p.nseg;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (p.seg_tile_start[mid] <= t) lo = mid; else hi = mid;
+      }
+      s_seg = lo;
+    }
+    __syncthreads();
+    const uint32_t s = s_seg;
+    const uint64_t b = p.seg_range[2 * s] + uint64_t(t - p.seg_tile_start[s]) * p.tile;
+    const uint64_t e = min(b + p.tile, p.seg_range[2 * s + 1]);
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+      const K v = kx.fwd(keys[i]);
+#pragma unroll
+      for (int d = 0; d < KD; ++d) atomicAdd(&s_h[d * RADIX + (uint32_t(v >> (8 * d)) & 255)], 1u);
+    }
+    __syncthreads();
+    uint32_t* g = p.hist + size_t(s) * KD * RADIX;
+    for (int i = threadIdx.x; i < KD * RADIX; i += blockDim.x)
+      if (s_h[i]) atomicAdd(&g[i], s_h[i]);
+    __syncthreads();
+  }
+}
+
+// In place: histogram -> exclusive bin bases, one block per segment.
+__global__ void __launch_bounds__(256) seg_scan_kernel(uint32_t* hist, uint32_t digits) {
+  __shared__ uint32_t s_tmp[8];
+  uint32_t* h = hist + size_t(blockIdx.x) * digits * RADIX;
+  for (uint32_t q = 0; q < digits; ++q) {
+    const uint32_t c = h[q * RADIX + threadIdx.x];
+    const uint32_t ex = block_excl_scan_256(c, s_tmp);
+    h[q * RADIX + threadIdx.x] = ex;
+  }
+}
+
+// Plan of a segmented pass sequence: every digit runs, counters cleared.
+__global__ void seg_plan_kernel(SortWork* w, uint32_t digits, uint32_t* gen_counter) {
+  const uint32_t t = threadIdx.x;
+  if (t < MAX_DIGITS) {
+    w->plan.tile_counter[t] = 0;
+    w->plan.exec_index[t] = t < digits ? t : PASS_SKIPPED;
+  }
+  if (t == 0) {
+    w->plan.m_exec = digits;
+    w->plan.gen_base = atomicAdd(gen_counter, uint32_t(MAX_DIGITS + 1));
+  }
+}
+
+}  // namespace gs
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct gs_seg_plan {
+  int key_bytes = 4;
+  uint32_t kind = 0;
+  bool desc = false;
+  uint64_t n = 0;
+  uint32_t ngroups = 0;
+  uint32_t nlarge = 0;
+  uint32_t large_tiles = 0;
+  uint32_t tile = 0;
+  int shape = 0;
+  gs::SegGroup* d_groups = nullptr;
+  uint32_t* d_starts_rel = nullptr;
+  uint32_t* d_tile_start = nullptr;
+  uint64_t* d_range = nullptr;
+  uint32_t* d_hist = nullptr;
+  gs::SortWork* d_work = nullptr;
+};
+
+namespace gs {
+
+// Build a plan from host offsets (nseg + 1 entries). Returns an error text
+// or empty on success.
+std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, uint64_t n,
+                           int key_bytes, uint32_t kind, bool desc, int shape) {
+  pl->key_bytes = key_bytes;
+  pl->kind = kind;
+  pl->desc = desc;
+  pl->n = n;
+  pl->shape = shape;
+  pl->tile = radix_shape_tile(key_bytes, 0, shape);
+  if (off[0] != 0 || off[nseg] != n) return "offsets must start at 0 and end at n";
+  std::vector<SegGroup> groups;
+  std::vector<uint32_t> rel;
+  std::vector<uint32_t> tile_start;
+  std::vector<uint64_t> range;
+  SegGroup cur{};
+  bool open = false;
+  auto close = [&]() {
+    if (open && cur.count > 0) {
+      rel.push_back(cur.count);  // end of the last segment
+      groups.push_back(cur);
+    } else if (open) {
+      rel.resize(cur.first_seg);  // empty group: drop its starts
+    }
+    open = false;
+  };
+  uint64_t tiles = 0;
+  for (uint32_t s = 0; s < nseg; ++s) {
+    const uint64_t b = off[s], e = off[s + 1];
+    if (e < b) return "offsets must be non-decreasing";
+    const uint64_t len = e - b;
+    if (len == 0) continue;  // nothing to move
+    if (len > GROUP_KEYS) {
+      close();
+      tile_start.push_back(uint32_t(tiles));
+      range.push_back(b);
+      range.push_back(e);
+      tiles += (len + pl->tile - 1) / pl->tile;
+      continue;
+    }
+    if (!open || cur.count + len > GROUP_KEYS || cur.nsegs + 1 > GROUP_MAX_SEGS ||
+        cur.start + cur.count != b) {
+      close();
+      cur = SegGroup{b, 0, uint32_t(rel.size()), 0, 0};
+      open = true;
+    }
+    rel.push_back(cur.count);
+    cur.count += uint32_t(len);
+    cur.nsegs += 1;
+  }
+  close();
+  if (tiles > 0xFFFFFFF0ull) return "too many tiles";
+  tile_start.push_back(uint32_t(tiles));
+  pl->ngroups = uint32_t(groups.size());
+  pl->nlarge = uint32_t(range.size() / 2);
+  pl->large_tiles = uint32_t(tiles);
+  auto up = [](void** dst, const void* src, size_t bytes) -> bool {
+    if (bytes == 0) return true;
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  bool ok = up(reinterpret_cast<void**>(&pl->d_groups), groups.data(), groups.size() * sizeof(SegGroup)) &&
+            up(reinterpret_cast<void**>(&pl->d_starts_rel), rel.data(), rel.size() * 4) &&
+            up(reinterpret_cast<void**>(&pl->d_tile_start), tile_start.data(), tile_start.size() * 4) &&
+            up(reinterpret_cast<void**>(&pl->d_range), range.data(), range.size() * 8);
+  if (ok && pl->nlarge) {
+    ok = cudaMalloc(&pl->d_hist, size_t(pl->nlarge) * key_bytes * RADIX * 4) == cudaSuccess &&
+         cudaMalloc(&pl->d_work, sizeof(SortWork)) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    return "device allocation for the segmented plan failed";
+  }
+  return "";
+}
+
+void seg_plan_free(gs_seg_plan* pl) {
+  void* ps[] = {pl->d_groups, pl->d_starts_rel, pl->d_tile_start, pl->d_range, pl->d_hist,
+                pl->d_work};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  delete pl;
+}
+
+gs_seg_plan* seg_plan_new() { return new gs_seg_plan(); }
+uint32_t seg_plan_large_tiles(const gs_seg_plan* pl) { return pl->large_tiles; }
+uint64_t seg_plan_n(const gs_seg_plan* pl) { return pl->n; }
+int seg_plan_key_bytes(const gs_seg_plan* pl) { return pl->key_bytes; }
+
+template <typename K>
+cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* alt,
+                      uint64_t* status, uint32_t* gen_counter, uint32_t* err, uint32_t spin_limit,
+                      const DeviceProps& props, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (pl->ngroups) {
+    GroupSortParams gp{in, out, pl->d_groups, pl->d_starts_rel, pl->kind, pl->desc};
+    constexpr size_t dyn = group_sort_dyn_smem<K>();
+    static bool attr = false;
+    if (!attr) {
+      e = cudaFuncSetAttribute(group_sort_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(dyn));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    group_sort_kernel<K><<<pl->ngroups, GROUP_THREADS, dyn, st>>>(gp);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (pl->nlarge == 0) return cudaSuccess;
+  const uint32_t digits = Bits<K>::DIGITS;
+  e = cudaMemsetAsync(pl->d_hist, 0, size_t(pl->nlarge) * digits * RADIX * 4, st);
+  if (e != cudaSuccess) return e;
+  SegHistParams hp{in, pl->d_tile_start, pl->d_range, pl->nlarge, pl->tile, pl->large_tiles,
+                   pl->kind, pl->desc, pl->d_hist};
+  unsigned hb = std::min<unsigned>(pl->large_tiles, unsigned(props.num_sms) * 8);
+  seg_hist_kernel<K><<<hb, 256, 0, st>>>(hp);
+  seg_scan_kernel<<<pl->nlarge, 256, 0, st>>>(pl->d_hist, digits);
+  seg_plan_kernel<<<1, 32, 0, st>>>(pl->d_work, digits, gen_counter);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  RadixJob job;
+  job.keys_in = in;
+  job.keys_out = out;
+  job.keys_alt = alt;
+  job.n = pl->n;
+  job.key_bytes = int(sizeof(K));
+  job.key_kind = pl->kind;
+  job.desc = pl->desc;
+  job.first_unstable = true;
+  job.status = status;
+  job.work = pl->d_work;
+  job.err = err;
+  job.spin_limit = spin_limit;
+  job.shape = pl->shape;
+  job.gen_counter = gen_counter;
+  SegJob sj{pl->d_tile_start, pl->d_range, pl->d_hist, pl->nlarge, digits, pl->large_tiles};
+  uint32_t unused = 0;
+  return launch_radix_passes(job, sj, props, &unused, st);
+}
+
+cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void* alt,
+                         uint64_t* status, uint32_t* gen_counter, uint32_t* err,
+                         uint32_t spin_limit, const DeviceProps& props, cudaStream_t st) {
+  if (pl->key_bytes == 4)
+    return seg_run_t<uint32_t>(pl, in, out, alt, status, gen_counter, err, spin_limit, props, st);
+  return seg_run_t<uint64_t>(pl, in, out, alt, status, gen_counter, err, spin_limit, props, st);
+}
+
+}  // namespace gs

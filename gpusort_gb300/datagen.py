@@ -142,3 +142,19 @@ def device(dist: str, n: int, dtype=np.uint32, seed: int = 0, device_index: int 
             if dist == "reverse":
                 a = torch.flip(a, dims=[0])
     return a.contiguous()
+
+
+def segment_offsets(nseg: int, lo: int = 16, hi: int = 1 << 22, total: int | None = None,
+                    seed: int = 8) -> np.ndarray:
+    """Offsets (nseg + 1, uint64) of segments with lengths log-uniform in
+    [lo, hi]. With `total`, lengths are scaled so they sum to about `total`
+    and clamped to at least `lo` (the batched workload's normalisation: the
+    unscaled mean on [16, 2^22] would give ~3.4e10 keys for 1e5 segments)."""
+    rng = np.random.default_rng(seed)
+    lens = np.exp(rng.uniform(np.log(lo), np.log(hi), size=nseg))
+    if total is not None:
+        lens = lens * (total / lens.sum())
+    lens = np.maximum(np.rint(lens), lo).astype(np.uint64)
+    off = np.zeros(nseg + 1, np.uint64)
+    np.cumsum(lens, out=off[1:])
+    return off

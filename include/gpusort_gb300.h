@@ -73,6 +73,7 @@ typedef enum gs_dtype {
 #define GS_FLAG_HOST         0x4u  /* pointers are host memory; synchronous */
 #define GS_FLAG_SYNC         0x8u  /* wait for completion and report
                                       GS_ERR_TIMEOUT from this call */
+#define GS_FLAG_OFFSETS_HOST 0x10u /* segment offsets are in host memory */
 
 /* Sorting strategy. Every strategy produces the same bytes. */
 typedef enum gs_algo {
@@ -147,14 +148,30 @@ gs_status gs_sort_pairs(gs_ctx* ctx, gs_dtype key_dtype, gs_dtype val_dtype,
                         uint32_t flags, const gs_opts* opts);
 
 /* Sort many independent segments in one call. Segment s is
- * [offsets[s], offsets[s+1]) of `in`; `offsets` has nseg+1 entries and is a
- * device pointer (host pointer with GS_FLAG_HOST), non-decreasing, with
- * offsets[0] == 0. Each segment is sorted on its own, as if it were one
- * rank's local sort (include/omp/omp_utils.h:147-207 applied per segment).
- * Empty segments are allowed. */
+ * [offsets[s], offsets[s+1]) of `in`; `offsets` has nseg+1 entries
+ * (device memory, or host memory with GS_FLAG_OFFSETS_HOST),
+ * non-decreasing, offsets[0] == 0 and offsets[nseg] == n. Each segment is
+ * sorted on its own, as one rank's local sort would be
+ * (include/omp/omp_utils.h:147-207 applied per segment). Empty segments are
+ * allowed. Keys only (32- or 64-bit types); `in` may equal `out`. With
+ * GS_FLAG_HOST, `in`/`out` are host memory. The call waits for completion. */
 gs_status gs_segmented_sort_keys(gs_ctx* ctx, gs_dtype dtype, const void* in,
                                  void* out, uint64_t n, const uint64_t* offsets,
                                  uint32_t nseg, uint32_t flags);
+
+/* The same work split in two: planning (host offsets; allocates the plan's
+ * device tables) and running (enqueues kernels only on the context's
+ * stream, no allocation and no host synchronisation, so a run can be
+ * captured into a CUDA graph and replayed). The context's scratch is sized
+ * for the plan when it is created. A plan may be run many times, on any
+ * device buffers of n keys; destroy it after its last run has completed. */
+typedef struct gs_seg_plan gs_seg_plan;
+gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
+                                   const uint64_t* host_offsets, uint32_t nseg,
+                                   uint32_t flags, gs_seg_plan** plan);
+gs_status gs_segmented_plan_run(gs_ctx* ctx, const gs_seg_plan* plan,
+                                const void* in, void* out);
+void gs_segmented_plan_destroy(gs_seg_plan* plan);
 
 /* Apply a permutation to a value array: out[i] = in[perm[i]], element size
  * `elem_bytes` (1..64 bytes). Replaces ParUtils::ArrangeValues

@@ -387,6 +387,21 @@ int oracle_sort_pairs(int kt, int vt, const void* kin, const void* vin, void* ko
   return ok ? 0 : -1;
 }
 
+// Batched sort: each segment [off[s], off[s+1]) sorted on its own, as each
+// rank's local sort is (include/omp/omp_utils.h:147-207).
+int oracle_segmented_sort_keys(int dtype, const void* in, void* out, uint64_t n,
+                               const uint64_t* off, uint32_t nseg, int desc) {
+  const size_t eb = (dtype <= F32) ? 4 : 8;
+  if (in != out) std::memcpy(out, in, n * eb);
+  uint8_t* base = static_cast<uint8_t*>(out);
+  for (uint32_t s = 0; s < nseg; ++s) {
+    const uint64_t b = off[s], e = off[s + 1];
+    if (e <= b) continue;
+    if (oracle_sort_keys(dtype, base + b * eb, base + b * eb, e - b, desc) != 0) return -1;
+  }
+  return 0;
+}
+
 // In-place HykSort of `n` keys over `p` thread-ranks (each rank gets the
 // contiguous slice [n*r/p, n*(r+1)/p)), k-way, `threads` workers per rank.
 // p or k not a power of two: the reference switches to SampleSort

@@ -42,7 +42,9 @@ def _load():
         L.oracle_sort_keys.argtypes = [i32, vp, vp, u64, i32]
         L.oracle_sort_pairs.argtypes = [i32, i32, vp, vp, vp, vp, u64, i32, i32]
         L.oracle_hyksort_cpu.argtypes = [i32, vp, u64, i32, i32, i32, u64, i32]
-        for f in ("oracle_sort_keys", "oracle_sort_pairs", "oracle_hyksort_cpu"):
+        L.oracle_segmented_sort_keys.argtypes = [i32, vp, vp, u64, vp, C.c_uint32, i32]
+        for f in ("oracle_sort_keys", "oracle_sort_pairs", "oracle_hyksort_cpu",
+                  "oracle_segmented_sort_keys"):
             getattr(L, f).restype = i32
         _lib = L
     return _lib
@@ -69,6 +71,18 @@ def sort_pairs(keys: np.ndarray, vals: np.ndarray, descending: bool = False,
                                    int(descending), int(stable))
     assert rc == 0
     return ko, vo
+
+
+def segmented_sort_keys(keys: np.ndarray, offsets: np.ndarray,
+                        descending: bool = False) -> np.ndarray:
+    """Each segment [offsets[s], offsets[s+1]) sorted on its own."""
+    a = np.ascontiguousarray(keys)
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    out = np.empty_like(a)
+    rc = _load().oracle_segmented_sort_keys(_CODES[a.dtype], a.ctypes.data, out.ctypes.data,
+                                            a.size, off.ctypes.data, off.size - 1, int(descending))
+    assert rc == 0
+    return out
 
 
 def hyksort_cpu(keys: np.ndarray, p: int = 4, k: int = 4, threads: int | None = None,
