@@ -1,6 +1,7 @@
 // C ABI of the engine (include/gpusort_gb300.h): contexts, scratch held
 // within an HBM budget, host staging, dispatch to the kernel launchers.
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -44,6 +45,7 @@ struct gs_ctx {
   DevBuf status;     // look-back words
   DevBuf alt_k, alt_v;
   DevBuf stage_k, stage_v, stage_off;
+  DevBuf splitters;  // sample sort
   // phase timing
   cudaEvent_t ev[8] = {};
   int n_phases = 0;
@@ -202,10 +204,135 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
   return GS_OK;
 }
 
+// Sort each of the given segments of `buf` in place (keys only); waits.
+gs_status sort_segments_in_place(gs_ctx* ctx, int kb, uint32_t kk, bool desc, void* buf,
+                                 uint64_t n, const std::vector<uint64_t>& off) {
+  gs_seg_plan* pl = gs::seg_plan_new();
+  const std::string err = gs::seg_plan_build(pl, off.data(), uint32_t(off.size() - 1), n, kb, kk,
+                                             desc, gs::radix_segmented_shape(kb));
+  if (!err.empty()) {
+    gs::seg_plan_free(pl);
+    return fail(ctx, GS_ERR_OOM, err);
+  }
+  gs_status st = prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX,
+                                uint32_t(kb));
+  if (st == GS_OK) {
+    cudaError_t e = gs::seg_plan_run(pl, buf, buf, ctx->alt_k.ptr,
+                                     static_cast<uint64_t*>(ctx->status.ptr),
+                                     &ctx->work->gen_counter, ctx->err, ctx->spin_limit,
+                                     ctx->props, ctx->stream);
+    if (e != cudaSuccess) st = cuda_fail(ctx, e, "segment sort launch");
+  }
+  cudaStreamSynchronize(ctx->stream);
+  gs::seg_plan_free(pl);
+  return st;
+}
+
+// SampleSort shape (keys only): splitters from an oversampled sample,
+// bucket scatter into p partitions, each partition sorted on its own.
+gs_status sample_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void* out,
+                             uint64_t n, uint32_t flags, const gs_opts* o) {
+  uint32_t p = (o && o->partitions) ? o->partitions : 64;
+  uint32_t os = (o && o->oversample) ? o->oversample : 32;
+  if (p > gs::RADIX) p = gs::RADIX;
+  if (p < 2) p = 2;
+  uint32_t samples = p * os;
+  if (samples > 8192) samples = 8192;
+  if (samples < p) samples = p;
+  const bool desc = flags & GS_FLAG_DESCENDING;
+  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st == GS_OK) st = ensure(ctx, ctx->splitters, gs::RADIX * 8);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0), 1);
+  if (st != GS_OK) return st;
+  const void* src = in;
+  if (in == out) {  // the bucket pass must not write its own input
+    cudaError_t e = cudaMemcpyAsync(ctx->alt_k.ptr, in, size_t(n) * kb, cudaMemcpyDeviceToDevice,
+                                    ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
+    src = ctx->alt_k.ptr;
+  }
+  gs::RadixJob job;
+  job.keys_in = src;
+  job.keys_out = out;
+  job.keys_alt = ctx->alt_k.ptr;
+  job.n = n;
+  job.key_bytes = kb;
+  job.key_kind = kk;
+  job.desc = desc;
+  job.first_unstable = true;
+  job.status = static_cast<uint64_t*>(ctx->status.ptr);
+  job.work = ctx->work;
+  job.err = ctx->err;
+  job.spin_limit = ctx->spin_limit;
+  gs::SampleJob sj{p, samples, o ? o->seed : 0, ctx->splitters.ptr};
+  cudaError_t e = gs::launch_sample_bucketing(job, sj, ctx->props, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sample bucketing launch");
+  std::vector<uint32_t> counts(p);
+  e = cudaMemcpyAsync(counts.data(), &ctx->work->hist[0][0], p * 4, cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "bucket sizes");
+  std::vector<uint64_t> off(p + 1, 0);
+  for (uint32_t i = 0; i < p; ++i) off[i + 1] = off[i] + counts[i];
+  if (off[p] != n) return fail(ctx, GS_ERR_CUDA, "bucket sizes do not add up to n");
+  phase_mark(ctx, "Exchange data");
+  return sort_segments_in_place(ctx, kb, kk, desc, out, n, off);
+}
+
+// HykSort shape (keys only): each of p partitions sorted on its own, then
+// merged by a tree of merge-path merges. p must be a power of two (the
+// reference falls back to SampleSort otherwise,
+// include/hyksort_common_vector.inl:31-43).
+gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void* out,
+                          uint64_t n, uint32_t flags, const gs_opts* o) {
+  uint32_t p = (o && o->partitions) ? o->partitions : 4;
+  const uint32_t k = (o && o->k_way) ? o->k_way : 4;
+  const bool pow2 = p && !(p & (p - 1)) && k && !(k & (k - 1));
+  if (!pow2) return sample_sort_device(ctx, kb, kk, in, out, n, flags, o);
+  const bool desc = flags & GS_FLAG_DESCENDING;
+  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st != GS_OK) return st;
+  const uint64_t run = (n + p - 1) / p;
+  std::vector<uint64_t> off(p + 1);
+  for (uint32_t i = 0; i <= p; ++i) off[i] = std::min<uint64_t>(uint64_t(i) * run, n);
+  if (in != out) {
+    cudaError_t e = cudaMemcpyAsync(out, in, size_t(n) * kb, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
+  }
+  st = sort_segments_in_place(ctx, kb, kk, desc, out, n, off);
+  if (st != GS_OK) return st;
+  phase_mark(ctx, "Local sort");
+  void* cur = out;
+  void* other = ctx->alt_k.ptr;
+  for (uint64_t r = run; r < n; r *= 2) {
+    cudaError_t e = gs::launch_merge_pass(cur, other, n, r, kb, kk, desc, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "merge launch");
+    std::swap(cur, other);
+  }
+  if (cur != out) {
+    cudaError_t e = cudaMemcpyAsync(out, cur, size_t(n) * kb, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
+  }
+  phase_mark(ctx, "Merge data");
+  return GS_OK;
+}
+
+// Strategy selection: SampleSort / HykSort shapes for keys, radix otherwise
+// (every strategy gives the same bytes).
+gs_status dispatch_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, const void* kin,
+                        const void* vin, void* kout, void* vout, uint64_t n, uint32_t flags,
+                        const gs_opts* opts) {
+  const uint32_t algo = opts ? opts->algo : GS_ALGO_AUTO;
+  if (vb == 0 && n >= 4096 && algo == GS_ALGO_SAMPLE)
+    return sample_sort_device(ctx, kb, kk, kin, kout, n, flags, opts);
+  if (vb == 0 && n >= 4096 && algo == GS_ALGO_HYK)
+    return hyk_sort_device(ctx, kb, kk, kin, kout, n, flags, opts);
+  return device_sort(ctx, kb, kk, vb, vk, kin, vin, kout, vout, n, flags);
+}
+
 gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const void* kin,
                       const void* vin, void* kout, void* vout, uint64_t n, uint32_t flags,
                       const gs_opts* opts) {
-  (void)opts;
   if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
   std::lock_guard<std::mutex> lock(ctx->mu);
   int kb = 0, vb = 0;
@@ -233,8 +360,8 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
       e = cudaMemcpyAsync(ctx->stage_v.ptr, vin, size_t(n) * vb, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "host to device copy");
     if (ctx->timing) { ctx->n_phases = 0; phase_mark(ctx, "Transfer in"); }
-    st = device_sort(ctx, kb, kk, vb, vk, ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr,
-                     ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr, n, flags);
+    st = dispatch_sort(ctx, kb, kk, vb, vk, ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr,
+                       ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr, n, flags, opts);
     if (st != GS_OK) return st;
     phase_mark(ctx, "Local sort");
     e = cudaMemcpyAsync(kout, ctx->stage_k.ptr, size_t(n) * kb, cudaMemcpyDeviceToHost, ctx->stream);
@@ -246,8 +373,8 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
   }
 
   if (ctx->timing) { cudaEventRecord(ctx->ev[0], ctx->stream); }
-  gs_status st = device_sort(ctx, kb, kk, vb, vk, kin, has_v ? vin : nullptr, kout,
-                             has_v ? vout : nullptr, n, flags);
+  gs_status st = dispatch_sort(ctx, kb, kk, vb, vk, kin, has_v ? vin : nullptr, kout,
+                               has_v ? vout : nullptr, n, flags, opts);
   if (st != GS_OK) return st;
   phase_mark(ctx, "Local sort");
   if (flags & GS_FLAG_SYNC) return check_err_word(ctx);
@@ -340,7 +467,7 @@ void gs_ctx_destroy(gs_ctx* ctx) {
   cudaSetDevice(ctx->props.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->status, &ctx->alt_k, &ctx->alt_v, &ctx->stage_k, &ctx->stage_v,
-                    &ctx->stage_off};
+                    &ctx->stage_off, &ctx->splitters};
   for (DevBuf* b : bufs) if (b->ptr) cudaFree(b->ptr);
   if (ctx->work) cudaFree(ctx->work);
   if (ctx->err) cudaFree(ctx->err);

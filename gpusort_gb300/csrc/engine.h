@@ -88,6 +88,25 @@ cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void*
                          uint64_t* status, uint32_t* gen_counter, uint32_t* err,
                          uint32_t spin_limit, const DeviceProps& props, cudaStream_t st);
 
+// Sample-sort bucketing (keys only): sample + splitters + bucket histogram
+// + one bucket scatter pass from job.keys_in to job.keys_out (which must
+// differ). job.work->hist[0][0..parts) holds the bucket sizes afterwards.
+struct SampleJob {
+  uint32_t parts;     // p buckets (2..256)
+  uint32_t samples;   // p * oversample (<= 8192)
+  uint64_t seed;
+  void* splitters;    // device buffer of >= 255 keys
+};
+cudaError_t launch_sample_bucketing(const RadixJob& job, const SampleJob& sj,
+                                    const DeviceProps& props, cudaStream_t st);
+cudaError_t launch_bucket_pass(const RadixJob& job, const void* splitters, uint32_t nsplit,
+                               const DeviceProps& props, cudaStream_t st);
+
+// One level of the merge tree: merge adjacent sorted runs of length `run`
+// of `in` (n keys, order of key_kind/desc) into runs of 2*run in `out`.
+cudaError_t launch_merge_pass(const void* in, void* out, uint64_t n, uint64_t run, int key_bytes,
+                              uint32_t key_kind, bool desc, cudaStream_t st);
+
 // Set the message gs_last_global_error() returns on this thread.
 void set_last_global_error(const std::string& msg);
 

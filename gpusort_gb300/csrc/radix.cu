@@ -70,18 +70,18 @@ template <typename K, typename V, int S> struct PassShape;
 // 256-thread pair variant raised an illegal-instruction fault on GB300
 // whose cause is not yet understood.
 template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 16, 2, 1> {};
-template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 24, 4, 1> {};
+template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 20, 4, 1> {};
 template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 16, 2, 8> {};
 template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 12, 2, 1> {};
-template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 16, 4, 1> {};
+template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4, 1> {};
 template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 12, 2, 8> {};
 template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 12, 2, 1> {};
 template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4, 1> {};
-template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 16, 4, 1> {};
+template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 10, 4, 1> {};
 template <typename K, typename V, int S>
-struct PassShape : Shape<(S == 0 ? 512 : 256), 8, (S == 0 ? 2 : 4), 1> {};
+struct PassShape : Shape<(S == 0 ? 512 : 256), (S == 0 ? 8 : 6), (S == 0 ? 2 : 4), 1> {};
 constexpr int NUM_SHAPES = 3;
-constexpr uint32_t MIN_TILE = 256 * 8;  // smallest tile of any shape
+constexpr uint32_t MIN_TILE = 1024;  // no shape has a smaller tile (smallest: 256 x 6)
 
 // Enqueue the digit passes (plan already in job.work). With `sj` the passes
 // sort the large segments of a batch; the shape must then run without
@@ -238,6 +238,54 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
     case 1: return launch_passes<uint64_t, NoValue, 1>(job, &sj, digits, 0, props, gen, stream);
     default: return cudaErrorInvalidValue;
   }
+}
+
+template <typename K>
+cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t nsplit,
+                          const DeviceProps& props, cudaStream_t st) {
+  using Sh = PassShape<K, NoValue, 0>;
+  static_assert(Sh::CLUSTER == 1, "bucket passes run without clusters");
+  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS>;
+  PlanParams pp{};
+  pp.work = job.work;
+  pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
+  pp.n = job.n;
+  pp.digits = 1;
+  pp.in_place = 0;
+  plan_kernel<<<1, 256, 0, st>>>(pp);
+  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, 1, true>;
+  static bool attr = false;
+  cudaError_t e = cudaSuccess;
+  if (!attr) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::DYN_SMEM));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  PassParams pa{};
+  pa.keys_in = job.keys_in;
+  pa.keys_out = job.keys_out;
+  pa.keys_alt = job.keys_alt;
+  pa.n = job.n;
+  pa.key_kind = job.key_kind;
+  pa.desc = job.desc;
+  pa.first_unstable = 1;
+  pa.status = job.status;
+  pa.spin_limit = job.spin_limit;
+  pa.inject_stall = job.inject_stall;
+  pa.work = job.work;
+  pa.err = job.err;
+  pa.pass = 0;
+  pa.splitters = splitters;
+  pa.nsplit = nsplit;
+  const uint64_t tiles = (job.n + Cfg::TILE - 1) / Cfg::TILE;
+  kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM, st>>>(pa);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_pass(const RadixJob& job, const void* splitters, uint32_t nsplit,
+                               const DeviceProps& props, cudaStream_t st) {
+  if (job.key_bytes == 4) return bucket_pass_t<uint32_t>(job, splitters, nsplit, props, st);
+  return bucket_pass_t<uint64_t>(job, splitters, nsplit, props, st);
 }
 
 uint32_t radix_tile(int key_bytes, int val_bytes) {

@@ -161,7 +161,8 @@ __device__ __forceinline__ void cluster_sync() {
   cluster_wait();
 }
 
-template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int CLUSTER>
+template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int CLUSTER,
+          bool BUCKET = false>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 pass_kernel(PassParams p) {
   using Cfg = PassConfig<K, V, THREADS, ITEMS>;
@@ -181,6 +182,7 @@ pass_kernel(PassParams p) {
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_seg;
+  __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode
   __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
   __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
 
@@ -270,6 +272,21 @@ pass_kernel(PassParams p) {
   const uint32_t tile_n =
       tile_base >= e1 ? 0u : uint32_t(e1 - tile_base < uint64_t(TILE) ? e1 - tile_base : uint64_t(TILE));
   const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
+  const uint32_t nsplit = p.nsplit;
+  if constexpr (BUCKET) {
+    for (uint32_t i = tid; i < nsplit; i += THREADS) s_split[i] = static_cast<const K*>(p.splitters)[i];
+    __syncthreads();
+  }
+  // Digit of order bits: a radix digit, or the bucket (upper_bound).
+  auto key_digit = [&](K y) -> uint32_t {
+    if constexpr (!BUCKET) return uint32_t(y >> shift) & (RADIX - 1);
+    uint32_t lo = 0, len = nsplit;
+    while (len > 0) {
+      const uint32_t half = len >> 1;
+      if (s_split[lo + half] <= y) { lo += half + 1; len -= half + 1; } else { len = half; }
+    }
+    return lo;
+  };
 
   // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
   // is input order and the stable ranking below keeps it.
@@ -304,7 +321,7 @@ pass_kernel(PassParams p) {
     if constexpr (HAS_V) {
       if (from_val) return uint32_t(vx.fwd(vals[i]) >> shift) & (RADIX - 1);
     }
-    return uint32_t(keys[i] >> shift) & (RADIX - 1);
+    return key_digit(keys[i]);
   };
 
   // Ranks are below the tile size (< 2^16): two per register.
@@ -471,10 +488,9 @@ pass_kernel(PassParams p) {
       VS v;
       if constexpr (HAS_V) {
         v = s_vals[r];
-        d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1))
-                     : (uint32_t(k >> shift) & (RADIX - 1));
+        d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1)) : key_digit(k);
       } else {
-        d = uint32_t(k >> shift) & (RADIX - 1);
+        d = key_digit(k);
       }
       const uint32_t dst = s_dst_base[d] + r;
       if (dst < n32) {

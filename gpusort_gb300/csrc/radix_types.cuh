@@ -69,6 +69,11 @@ struct PassParams {
   const uint32_t* seg_binbase;
   uint32_t nseg;
   uint32_t seg_digits;
+  // Bucket mode (sample sort): the "digit" of a key is the number of
+  // splitters not greater than its order bits (upper_bound), i.e. its bucket
+  // among nsplit + 1 <= RADIX buckets; splitters are sorted order bits.
+  const void* splitters;
+  uint32_t nsplit;
 };
 
 }  // namespace gs
