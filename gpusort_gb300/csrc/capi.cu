@@ -613,15 +613,36 @@ gs_status gs_gather(gs_ctx* ctx, const void* in, void* out, uint64_t n, uint32_t
   if (n == 0) return GS_OK;
   if (!in || !out || !perm || elem_bytes == 0 || elem_bytes > 64)
     return fail(ctx, GS_ERR_INVALID, "bad gather arguments");
-  if (flags & GS_FLAG_HOST) return fail(ctx, GS_ERR_INVALID, "gather takes device pointers");
   cudaSetDevice(ctx->props.device);
+  const void* din = in;
+  void* dout = out;
+  const uint64_t* dperm = perm;
+  const size_t bytes = size_t(n) * elem_bytes;
+  if (flags & GS_FLAG_HOST) {  // stage: values in stage_k, perm in stage_off, result in alt_k
+    gs_status st = ensure(ctx, ctx->stage_k, bytes);
+    if (st == GS_OK) st = ensure(ctx, ctx->stage_off, size_t(n) * 8);
+    if (st == GS_OK) st = ensure(ctx, ctx->alt_k, bytes);
+    if (st != GS_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(ctx->stage_k.ptr, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ctx->stage_off.ptr, perm, size_t(n) * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "host to device copy");
+    din = ctx->stage_k.ptr;
+    dout = ctx->alt_k.ptr;
+    dperm = static_cast<const uint64_t*>(ctx->stage_off.ptr);
+  }
   unsigned blocks = unsigned((n + 255) / 256);
   const unsigned cap = unsigned(ctx->props.num_sms) * 8;
   if (blocks > cap) blocks = cap;
-  gather_kernel<<<blocks, 256, 0, ctx->stream>>>(static_cast<const uint8_t*>(in),
-                                                 static_cast<uint8_t*>(out), n, elem_bytes, perm);
+  gather_kernel<<<blocks, 256, 0, ctx->stream>>>(static_cast<const uint8_t*>(din),
+                                                 static_cast<uint8_t*>(dout), n, elem_bytes, dperm);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "gather launch");
+  if (flags & GS_FLAG_HOST) {
+    e = cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device to host copy");
+    return check_err_word(ctx);
+  }
   if (flags & GS_FLAG_SYNC) return check_err_word(ctx);
   return GS_OK;
 }

@@ -176,7 +176,9 @@ void gs_segmented_plan_destroy(gs_seg_plan* plan);
 /* Apply a permutation to a value array: out[i] = in[perm[i]], element size
  * `elem_bytes` (1..64 bytes). Replaces ParUtils::ArrangeValues
  * (include/par/par_utils.h:23-86), which moves each value vector to where
- * its key went after a sort of (key, global index). */
+ * its key went after a sort of (key, global index). Device pointers, or
+ * host pointers (values, result and perm) with GS_FLAG_HOST; `in` and
+ * `out` must not alias. */
 gs_status gs_gather(gs_ctx* ctx, const void* in, void* out, uint64_t n,
                     uint32_t elem_bytes, const uint64_t* perm, uint32_t flags);
 
