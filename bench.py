@@ -17,6 +17,18 @@ ascending, inputs resident in HBM. A step is one full sort of the array.
   cpu_baseline the reference's CPU HykSort (k=4 over 4 thread-ranks, merge
                sort local sort) restated in oracle/, timed on a bounded
                sample of the same workload on the host cores
+  secondary    the other single-GPU workloads, device-resident, CUDA events:
+               2^29 float32 N(0,1) (radix, and the SampleSort shape with
+               p=64, oversampling 32); 2^29 uint64 Zipf(1.1) keys with a
+               uint32 index payload, stable; 100,000 uint32 segments of
+               log-uniform length in [16, 2^22] scaled to ~2^30 keys, one
+               planned batched sort replayed from a CUDA graph
+  serving      Poisson arrivals of the serving mix (sizes log-uniform in
+               [2^10, 2^26]; 40% u32, 30% u64, 20% f32, 10% i64+u32 pairs),
+               120 GB admission budget: the server (gs_server_*) against one
+               plain synchronous sort call per request, closed loop and at
+               0.3/0.6/0.9/1.2x the plain arm's request rate; p50/p99 of
+               submit -> completion
 
 `--impl reference` runs only that CPU path and prints its own line.
 With torchrun and N>1 every rank sorts its own array (replicas).
@@ -54,6 +66,10 @@ def parse():
                     help="bound on the CPU baseline's sampled work")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-slots", type=int, default=8)
     return ap.parse_args()
 
 
@@ -134,7 +150,7 @@ def cpu_baseline(keys_sample: np.ndarray, budget_s: float, threads_total: int | 
         t0 = time.perf_counter()
         out = oracle.hyksort_cpu(keys_sample, p=4, k=4, threads=per_rank, seed=1)
         times.append(time.perf_counter() - t0)
-        if time.perf_counter() > t_end or len(times) >= 5:
+        if time.perf_counter() > t_end or len(times) >= 30:
             break
     t = statistics.median(times)
     ok = bool(np.all(out[1:] >= out[:-1]))
@@ -142,6 +158,145 @@ def cpu_baseline(keys_sample: np.ndarray, budget_s: float, threads_total: int | 
             "kind": "port", "sample": f"{keys_sample.size} uint32 uniform keys "
             f"(k=4 HykSort over 4 thread-ranks x {per_rank} threads, median of {len(times)})",
             "seconds": t, "sorted": ok}
+
+
+def time_steps(fn, stream, steps: int, warmup: int) -> float:
+    """Average ms of fn() over `steps` runs after `warmup`, CUDA events on
+    `stream` (the stream the engine launches on)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _unsigned_sorted(t, wide: bool) -> bool:
+    import torch
+    sign = torch.tensor(-2**63 if wide else -2**31, dtype=t.dtype, device=t.device)
+    s = t ^ sign
+    return bool((s[1:] >= s[:-1]).all())
+
+
+def secondary(ctx, stream, pk: dict, steps: int, warmup: int) -> dict:
+    import torch
+    from gpusort_gb300 import capi, datagen
+    out = {}
+    hbm = pk["hbm_gbs"]
+
+    def ok(st):
+        if st != capi.GS_OK:
+            raise RuntimeError(ctx.last_error())
+
+    # float32 N(0,1), 2^29 keys: radix, and the SampleSort shape (p=64, x32)
+    n = 1 << 29
+    f = datagen.device("normal", n, np.float32, seed=2)
+    fo = torch.empty_like(f)
+    for name, kw in (("radix", {}),
+                     ("samplesort_p64_os32", {"algo": capi.ALGO_SAMPLE, "partitions": 64,
+                                              "oversample": 32})):
+        ms = time_steps(lambda: ok(ctx.sort_keys(f, fo, dtype=np.float32, **kw)), stream,
+                        steps, warmup)
+        ctx.synchronize()
+        out[f"f32_normal_2^29_{name}"] = {
+            "gkeys_s": n / ms / 1e6, "ms": ms, "frac_36B": 36 * n / ms / 1e6 / hbm,
+            "sorted": bool((fo[1:] >= fo[:-1]).all()),
+            "sum_preserved": bool(torch.isclose(fo.double().sum(), f.double().sum()))}
+    del f, fo
+
+    # uint64 Zipf(1.1) keys + uint32 index, stable, 2^29 pairs
+    k = datagen.device("zipf", n, np.uint64, seed=3)
+    v = torch.arange(n, dtype=torch.int32, device=k.device)
+    ko, vo = torch.empty_like(k), torch.empty_like(v)
+    ms = time_steps(lambda: ok(ctx.sort_pairs(k, v, ko, vo, key_dtype=np.uint64,
+                                              val_dtype=np.uint32, stable=True)),
+                    stream, steps, warmup)
+    ctx.synchronize()
+    ties = ko[1:] == ko[:-1]
+    out["u64_zipf_2^29_pairs_u32_stable"] = {
+        "gkeys_s": n / ms / 1e6, "ms": ms, "frac_200B": 200 * n / ms / 1e6 / hbm,
+        "sorted": _unsigned_sorted(ko, True),
+        "ties_in_input_order": bool((vo[1:][ties] > vo[:-1][ties]).all()),
+        "payload_permutation": int(vo.to(torch.int64).sum()) == n * (n - 1) // 2}
+    del k, v, ko, vo
+
+    # batched segmented sort: 100,000 segments, ~2^30 keys, CUDA graph
+    off = datagen.segment_offsets(100000, 16, 1 << 22, total=1 << 30, seed=8)
+    ns = int(off[-1])
+    a = datagen.device("uniform", ns, np.uint32, seed=8)
+    ao = torch.empty_like(a)
+    plan = ctx.segmented_plan(np.uint32, ns, off)
+    side = torch.cuda.Stream()
+    try:
+        ctx.set_stream(side.cuda_stream)
+        ok(ctx.segmented_run(plan, a, ao))  # eager run before capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            ok(ctx.segmented_run(plan, a, ao))
+        with torch.cuda.stream(side):  # replay() launches on the current stream
+            ms = time_steps(g.replay, side, steps, warmup)
+        ok(ctx.status_synchronize())
+    finally:
+        ctx.set_stream(stream.cuda_stream)
+        ctx.segmented_destroy(plan)
+    s32 = ao ^ torch.tensor(-2**31, dtype=torch.int32, device=ao.device)
+    inner = torch.ones(ns - 1, dtype=torch.bool, device=ao.device)
+    bounds = torch.from_numpy(off[1:-1].astype(np.int64) - 1).to(ao.device)
+    inner[bounds[(bounds >= 0) & (bounds < ns - 1)]] = False
+    out["segmented_100k_u32"] = {
+        "keys": ns, "segments": 100000, "gkeys_s": ns / ms / 1e6, "ms": ms,
+        "frac_36B": 36 * ns / ms / 1e6 / hbm, "graph": True,
+        "segments_sorted": bool((s32[1:] >= s32[:-1])[inner].all())}
+    del a, ao, g
+    torch.cuda.empty_cache()
+    return out
+
+
+def serving_bench(ctx, count: int, slots: int) -> dict:
+    import torch
+    from gpusort_gb300 import capi, serving
+    specs = serving.request_mix(count, seed=5)
+    reqs = [serving.DeviceRequest(s) for s in specs]
+    res = {"requests": count, "keys": sum(s.n for s in specs), "slots": slots,
+           "hbm_budget_gb": 120, "latency": "submit -> completion, ms"}
+    with capi.Server(0, hbm_budget=120 << 30, max_request_keys=1 << 26, slots=slots) as srv:
+        serving.run_plain(ctx, reqs[:20], None)      # warm-up of both arms
+        serving.run_served(srv, reqs[:20], None)
+        plain = serving.run_plain(ctx, reqs, None)
+        served = serving.run_served(srv, reqs, None)
+        res["closed_loop"] = {"plain": plain, "served": served,
+                              "throughput_ratio": served["gkeys_s"] / plain["gkeys_s"]}
+        rate = count / plain["wall_s"]
+        sweep = []
+        for m in (0.3, 0.6, 0.9, 1.2):
+            arr = serving.poisson_arrivals(count, m * rate, seed=6)
+            p = serving.run_plain(ctx, reqs, arr)
+            s = serving.run_served(srv, reqs, arr)
+            sweep.append({"load": m, "rate_req_s": m * rate,
+                          "plain": {k: p[k] for k in ("p50_ms", "p99_ms", "gkeys_s")},
+                          "served": {k: s[k] for k in ("p50_ms", "p99_ms", "gkeys_s")}})
+        res["poisson"] = sweep
+        res["arena_peak_gb"] = srv.stats()["arena_peak"] / 1e9
+    # served outputs equal the plain ones (last writer was the served arm)
+    same = True
+    for r in reqs[: min(count, 40)]:
+        ko = r.keys_out.clone()
+        vo = r.vals_out.clone() if r.vals is not None else None
+        r.sort_plain(ctx)
+        same &= bool(torch.equal(ko, r.keys_out))
+        if vo is not None:
+            same &= bool(torch.equal(vo, r.vals_out))
+    res["served_equals_plain_first40"] = same
+    del reqs
+    torch.cuda.empty_cache()
+    return res
 
 
 def run_reference(args):
@@ -286,8 +441,16 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        sample = keys[: 1 << 24].cpu().numpy().view(np.uint32).copy()
+        sample = keys[: 1 << 26].cpu().numpy().view(np.uint32).copy()
         cpu = cpu_baseline(sample, args.cpu_seconds)
+    del keys, out
+    torch.cuda.empty_cache()
+    sec = None
+    if not args.no_secondary:
+        sec = secondary(ctx, stream, pk, steps=5, warmup=3)
+    srv = None
+    if not args.no_serving:
+        srv = serving_bench(ctx, args.serve_requests, args.serve_slots)
 
     line = {
         "metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world,
@@ -310,6 +473,8 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": args.steps * 6,
         "checks": {"sorted": sorted_ok, "sum_preserved": ksum == osum},
+        "secondary": sec,
+        "serving": srv,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

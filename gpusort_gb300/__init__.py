@@ -7,6 +7,6 @@ built for sm_103a by ``gpusort_gb300._build``) behind the C ABI in
 that ABI for tests and benchmarks; the C++ drop-in headers live in
 ``include/gpusort/``.
 """
-from .capi import Context, GsError, load  # noqa: F401
+from .capi import Context, GsError, Server, load  # noqa: F401
 
-__all__ = ["Context", "GsError", "load"]
+__all__ = ["Context", "GsError", "Server", "load"]

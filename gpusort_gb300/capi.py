@@ -25,6 +25,7 @@ GS_ERR_INVALID = 6
 GS_ERR_NO_DEVICE = 7
 GS_ERR_TOO_LARGE = 8
 GS_ERR_BUSY = 9
+GS_ERR_CANCELLED = 10
 
 # gs_dtype
 GS_U32, GS_I32, GS_F32, GS_U64, GS_I64, GS_F64 = range(6)
@@ -50,6 +51,8 @@ EXPORTED = [
     "gs_segmented_sort_keys", "gs_gather", "gs_phase_times",
     "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set", "gs_sort_keys_noalloc",
     "gs_segmented_plan_create", "gs_segmented_plan_run", "gs_segmented_plan_destroy",
+    "gs_server_create", "gs_server_destroy", "gs_server_submit", "gs_server_poll",
+    "gs_server_cancel", "gs_server_get_stats",
 ]
 
 _NP_DTYPE = {
@@ -61,6 +64,18 @@ _NP_DTYPE = {
 class gs_opts(C.Structure):
     _fields_ = [("algo", C.c_uint32), ("partitions", C.c_uint32), ("k_way", C.c_uint32),
                 ("oversample", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class gs_server_opts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_request_keys", C.c_uint64),
+                ("slots", C.c_uint32), ("max_queue", C.c_uint32)]
+
+
+class gs_server_stats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("keys_done", C.c_uint64), ("queued", C.c_uint64),
+                ("running", C.c_uint64), ("arena_used", C.c_uint64), ("arena_peak", C.c_uint64),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double)]
 
 
 class GsError(RuntimeError):
@@ -121,6 +136,19 @@ def load() -> C.CDLL:
         L.gs_segmented_plan_destroy.restype = None
         L.gs_sort_keys_noalloc.argtypes = [i32, vp, vp, u64, u32, vp]
         L.gs_sort_keys_noalloc.restype = i32
+        L.gs_server_create.argtypes = [i32, C.POINTER(gs_server_opts)]
+        L.gs_server_create.restype = vp
+        L.gs_server_destroy.argtypes = [vp]
+        L.gs_server_destroy.restype = None
+        L.gs_server_submit.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, u64, u32,
+                                       C.POINTER(u64)]
+        L.gs_server_submit.restype = i32
+        L.gs_server_poll.argtypes = [vp, u64, i32, C.POINTER(C.c_double)]
+        L.gs_server_poll.restype = i32
+        L.gs_server_cancel.argtypes = [vp, u64]
+        L.gs_server_cancel.restype = i32
+        L.gs_server_get_stats.argtypes = [vp, C.POINTER(gs_server_stats), i32]
+        L.gs_server_get_stats.restype = i32
         for fn in ("gs_ctx_set_stream", "gs_ctx_synchronize", "gs_sort_keys", "gs_sort_pairs",
                    "gs_segmented_sort_keys", "gs_gather", "gs_ctx_set_timing", "gs_debug_set"):
             getattr(L, fn).restype = i32
@@ -268,3 +296,66 @@ class Context:
 
     def debug_set(self, key: int, value: int):
         self._check(self.L.gs_debug_set(self.h, key, value))
+
+
+class Server:
+    """Serving loop on one device (gs_server_*): submit sort requests, poll
+    their completion. Device tensors by default; host arrays with FLAG_HOST."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, max_request_keys: int = 0,
+                 slots: int = 0, max_queue: int = 0):
+        self.L = load()
+        o = gs_server_opts(hbm_budget, max_request_keys, slots, max_queue)
+        h = self.L.gs_server_create(device, C.byref(o))
+        if not h:
+            raise GsError(GS_ERR_NO_DEVICE, self.L.gs_last_global_error().decode())
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gs_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, keys_in, keys_out, vals_in=None, vals_out=None, *, descending=False,
+               stable=False, flags=0, n=None, key_dtype=None, val_dtype=None) -> int:
+        """Queue one request; returns its id. Raises GsError on refusal."""
+        n = _count(keys_in) if n is None else int(n)
+        f = flags | (FLAG_DESCENDING if descending else 0) | (FLAG_PAIRS_STABLE if stable else 0)
+        kc = dtype_code(key_dtype if key_dtype is not None else keys_in.dtype)
+        has_v = vals_in is not None
+        vc = dtype_code(val_dtype if val_dtype is not None else vals_in.dtype) if has_v else 0
+        rid = C.c_uint64()
+        st = self.L.gs_server_submit(self.h, kc, int(has_v), vc, _ptr(keys_in), _ptr(vals_in),
+                                     _ptr(keys_out), _ptr(vals_out), n, f, C.byref(rid))
+        if st != GS_OK:
+            raise GsError(st, self.L.gs_last_global_error().decode())
+        return rid.value
+
+    def poll(self, request_id: int, wait: bool = True) -> tuple[int, float]:
+        """(status, latency ms); status GS_ERR_BUSY while not finished."""
+        ms = C.c_double()
+        st = self.L.gs_server_poll(self.h, request_id, int(wait), C.byref(ms))
+        return st, ms.value
+
+    def cancel(self, request_id: int) -> int:
+        return self.L.gs_server_cancel(self.h, request_id)
+
+    def stats(self, reset: bool = False) -> dict:
+        s = gs_server_stats()
+        st = self.L.gs_server_get_stats(self.h, C.byref(s), int(reset))
+        if st != GS_OK:
+            raise GsError(st, "stats")
+        return {k: getattr(s, k) for k, _ in gs_server_stats._fields_}

@@ -42,7 +42,8 @@ typedef enum gs_status {
   GS_ERR_INVALID = 6,      /* bad argument (null pointer, bad option) */
   GS_ERR_NO_DEVICE = 7,    /* no CUDA device (src/cuda_utils.cu:81-92) */
   GS_ERR_TOO_LARGE = 8,    /* n beyond the engine's per-call limit */
-  GS_ERR_BUSY = 9          /* serving queue full / request not finished */
+  GS_ERR_BUSY = 9,         /* serving queue full / request not finished */
+  GS_ERR_CANCELLED = 10    /* serving request cancelled before it ran */
 } gs_status;
 
 /* Key and value element types: the reference's instantiation set
@@ -233,6 +234,67 @@ gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 #define GS_NOALLOC_MAX_KEYS (1ull << 20)
 gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out,
                                uint64_t n, uint32_t flags, void* stream);
+
+/* ---- Serving loop (continuous batching) ----
+ * No counterpart in the reference (its callers sort one array per call,
+ * src/test/utils.h:776-791); the request interface follows the sort calls
+ * above. A server owns one device:
+ * - an HBM arena of `hbm_budget` bytes, allocated once, from which each
+ *   admitted request takes its scratch (and, with GS_FLAG_HOST, its staged
+ *   data); admission waits while the arena is full, so the budget bounds
+ *   the device memory of everything in flight;
+ * - `slots` CUDA streams, each with its own look-back words and work area;
+ * - one device-owner thread that admits queued requests in arrival order as
+ *   slots and arena space free up (a request that does not fit yet holds
+ *   the head of the queue), so work of requests that arrive while others
+ *   run overlaps on the device.
+ * Requests are sorts of keys or (key, value) pairs with the flags of
+ * gs_sort_pairs (GS_FLAG_DESCENDING, GS_FLAG_PAIRS_STABLE). By default the
+ * pointers are device memory on the server's device, which stays the
+ * caller's until the request completes (keys_out may equal keys_in); with
+ * GS_FLAG_HOST they are host memory (pinned memory lets the copies overlap)
+ * and the server copies in and out. Results are the bytes gs_sort_pairs /
+ * gs_sort_keys return for the same input. */
+typedef struct gs_server gs_server;
+typedef struct gs_server_opts {
+  uint64_t hbm_budget;        /* arena bytes (0: 1 GiB) */
+  uint64_t max_request_keys;  /* largest n accepted (0: 2^26) */
+  uint32_t slots;             /* requests on the device at once (0: 8; <= 32) */
+  uint32_t max_queue;         /* queued requests before submit returns
+                                 GS_ERR_BUSY (0: 65536) */
+} gs_server_opts;
+
+typedef struct gs_server_stats {
+  uint64_t completed;         /* requests finished since the last reset */
+  uint64_t keys_done;         /* their keys */
+  uint64_t queued;            /* waiting for admission now */
+  uint64_t running;           /* admitted, not finished */
+  uint64_t arena_used;        /* arena bytes held now */
+  uint64_t arena_peak;        /* most arena bytes held since the last reset */
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> completion */
+} gs_server_stats;
+
+/* Returns NULL on failure (gs_last_global_error() says why). */
+gs_server* gs_server_create(int device, const gs_server_opts* opts);
+/* Cancels queued requests, waits for admitted ones, frees everything. */
+void gs_server_destroy(gs_server* server);
+/* Queue one request; *request_id identifies it for poll/cancel. Errors:
+ * GS_ERR_EMPTY (n == 0), GS_ERR_TOO_LARGE (n > max_request_keys),
+ * GS_ERR_OOM (needs more than the whole arena), GS_ERR_BUSY (queue full). */
+gs_status gs_server_submit(gs_server* server, gs_dtype key_dtype, int has_values,
+                           gs_dtype val_dtype, const void* keys_in, const void* vals_in,
+                           void* keys_out, void* vals_out, uint64_t n, uint32_t flags,
+                           uint64_t* request_id);
+/* GS_ERR_BUSY while the request is queued or running (wait = 0), else its
+ * final status (GS_OK, GS_ERR_TIMEOUT, GS_ERR_CUDA, GS_ERR_CANCELLED); the
+ * final status is returned once, after which the id is unknown
+ * (GS_ERR_INVALID). latency_ms (may be NULL) gets submit -> completion. */
+gs_status gs_server_poll(gs_server* server, uint64_t request_id, int wait, double* latency_ms);
+/* Cancel a request that is still queued (GS_OK); GS_ERR_BUSY if it was
+ * already admitted (it then runs to completion). */
+gs_status gs_server_cancel(gs_server* server, uint64_t request_id);
+/* Snapshot of the counters; reset != 0 clears completed/keys/latencies/peak. */
+gs_status gs_server_get_stats(gs_server* server, gs_server_stats* out, int reset);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -1,5 +1,6 @@
 """CPU-only checks of the C ABI library: it builds, loads, and exports every
 function include/gpusort_gb300.h declares. No compute call is made."""
+import ctypes as C
 import re
 from pathlib import Path
 
@@ -41,3 +42,23 @@ def test_null_context_is_rejected(built_lib):
     o = capi.gs_opts()
     assert L.gs_sort_keys(None, capi.GS_U32, None, None, 10, 0, o) == capi.GS_ERR_INVALID
     assert L.gs_ctx_synchronize(None) == capi.GS_ERR_INVALID
+
+
+def test_server_needs_a_device(built_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = capi.load()
+    o = capi.gs_server_opts(1 << 20, 0, 2, 0)
+    assert L.gs_server_create(0, o) is None
+    assert b"no such CUDA device" in L.gs_last_global_error()
+    with pytest.raises(capi.GsError):
+        capi.Server(0)
+    stats = capi.gs_server_stats()
+    assert L.gs_server_get_stats(None, stats, 0) == capi.GS_ERR_INVALID
+    assert L.gs_server_poll(None, 1, 0, None) == capi.GS_ERR_INVALID
+    assert L.gs_server_cancel(None, 1) == capi.GS_ERR_INVALID
+    rid = C.c_uint64()
+    assert L.gs_server_submit(None, capi.GS_U32, 0, 0, None, None, None, None, 10, 0,
+                              rid) == capi.GS_ERR_INVALID
+    L.gs_server_destroy(None)
