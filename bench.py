@@ -51,8 +51,13 @@ sys.path.insert(0, str(ROOT))
 
 B_ALG_PER_KEY_U32 = 36          # 4 * (2 * 4 + 1): histogram read + 4 passes
 PASS_BYTES_PER_KEY_U32 = 8      # one pass reads and writes each 4-byte key
+# DRAM bytes per key of one stable pass launch, from the ncu capture of a
+# 2^26-key sort (dram__bytes_read.sum + dram__bytes_write.sum = 516.4 MB per
+# launch, profiles/pass_kernel_u32_2e26_full.md); traffic is per key
+# (streaming reads and writes), so it scales to 2^30 by the key count.
+PASS_TRAFFIC_PER_KEY_U32 = 516.4e6 / (1 << 26)
 METRIC = "sort throughput (Gkeys/s)"
-WORKLOAD = "single-array sort, 2^30 uint32 keys uniform over [0, 2^32), ascending"
+WORKLOAD = "single-array sort, 2^{} uint32 keys uniform over [0, 2^32), ascending"
 
 
 def parse():
@@ -324,7 +329,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_keys": n, "ranks": 4, "k_way": 4,
+        "config": {"workload": WORKLOAD.format(args.log2n), "sample_keys": n, "ranks": 4, "k_way": 4,
                    "threads_per_rank": per_rank},
         "cpu_baseline": {"value": v, "unit": "Gkeys/s", "cores": per_rank * 4, "kind": "port",
                          "sample": f"{n} of the 2^{args.log2n} uint32 uniform keys per step "
@@ -457,12 +462,14 @@ def main():
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": t_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "key": "uint32", "algo": "radix (onesweep LSD)",
+        "config": {"workload": WORKLOAD.format(args.log2n), "n": n, "key": "uint32", "algo": "radix (onesweep LSD)",
                    "l2": "inputs 4 GiB > 129 MB L2, no flush needed",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": "pass_kernel (one onesweep digit pass)",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "frac": achieved / pk["hbm_gbs"],
+                     "traffic": PASS_TRAFFIC_PER_KEY_U32 * n,
+                     "traffic_source": "ncu dram bytes of a 2^26-key pass, scaled by keys",
                      "peak_source": pk["source"], "bytes_per_launch": pass_alg,
                      "launch_ms": pass_avg},
         "sort_roofline": {"achieved": sort_achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
