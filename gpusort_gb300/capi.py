@@ -53,6 +53,10 @@ EXPORTED = [
     "gs_segmented_plan_create", "gs_segmented_plan_run", "gs_segmented_plan_destroy",
     "gs_server_create", "gs_server_destroy", "gs_server_submit", "gs_server_poll",
     "gs_server_cancel", "gs_server_get_stats",
+    "gs_pass_shape_count", "gs_pass_shape_info", "gs_ctx_set_tuning", "gs_tuning_parse",
+    "gs_ctx_load_tuning", "gs_ctx_choice",
+    "gs_file_count", "gs_file_read", "gs_file_write", "gs_partitions_read",
+    "gs_partitions_write", "gs_partition_block",
 ]
 
 _NP_DTYPE = {
@@ -64,6 +68,14 @@ _NP_DTYPE = {
 class gs_opts(C.Structure):
     _fields_ = [("algo", C.c_uint32), ("partitions", C.c_uint32), ("k_way", C.c_uint32),
                 ("oversample", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class gs_tuning_entry(C.Structure):
+    _fields_ = [("key_dtype", C.c_int32), ("val_bytes", C.c_int32), ("log2n_min", C.c_uint32),
+                ("log2n_max", C.c_uint32), ("pass_shape", C.c_int32), ("partitions", C.c_uint32)]
+
+
+DTYPE_NAMES = ["u32", "i32", "f32", "u64", "i64", "f64"]
 
 
 class gs_server_opts(C.Structure):
@@ -136,6 +148,30 @@ def load() -> C.CDLL:
         L.gs_segmented_plan_destroy.restype = None
         L.gs_sort_keys_noalloc.argtypes = [i32, vp, vp, u64, u32, vp]
         L.gs_sort_keys_noalloc.restype = i32
+        L.gs_pass_shape_count.restype = i32
+        L.gs_pass_shape_info.argtypes = [i32, i32, i32, C.POINTER(u32), C.POINTER(u32)]
+        L.gs_pass_shape_info.restype = i32
+        L.gs_ctx_set_tuning.argtypes = [vp, C.POINTER(gs_tuning_entry), u32]
+        L.gs_ctx_set_tuning.restype = i32
+        L.gs_tuning_parse.argtypes = [C.c_char_p, C.POINTER(gs_tuning_entry), u32]
+        L.gs_tuning_parse.restype = i32
+        L.gs_ctx_load_tuning.argtypes = [vp, C.c_char_p]
+        L.gs_ctx_load_tuning.restype = i32
+        L.gs_ctx_choice.argtypes = [vp, i32, i32, u64, C.POINTER(C.c_int), C.POINTER(u32)]
+        L.gs_ctx_choice.restype = i32
+        L.gs_file_count.argtypes = [C.c_char_p]
+        L.gs_file_count.restype = C.c_int64
+        L.gs_file_read.argtypes = [vp, C.c_char_p, vp, u64, u32, u32, C.POINTER(u64)]
+        L.gs_file_read.restype = i32
+        L.gs_file_write.argtypes = [vp, C.c_char_p, vp, u64, u32, u32]
+        L.gs_file_write.restype = i32
+        L.gs_partitions_read.argtypes = [vp, C.c_char_p, C.c_char_p, i32, vp, u64, u32, u32,
+                                         C.POINTER(u64)]
+        L.gs_partitions_read.restype = i32
+        L.gs_partitions_write.argtypes = [vp, C.c_char_p, C.c_char_p, i32, vp, u64, u32, u32]
+        L.gs_partitions_write.restype = i32
+        L.gs_partition_block.argtypes = [u64, i32]
+        L.gs_partition_block.restype = u64
         L.gs_server_create.argtypes = [i32, C.POINTER(gs_server_opts)]
         L.gs_server_create.restype = vp
         L.gs_server_destroy.argtypes = [vp]
@@ -154,6 +190,37 @@ def load() -> C.CDLL:
             getattr(L, fn).restype = i32
         _lib = L
         return L
+
+
+def _entry(e: dict) -> gs_tuning_entry:
+    kd = e["key_dtype"]
+    kd = DTYPE_NAMES.index(kd) if isinstance(kd, str) else int(kd)
+    return gs_tuning_entry(kd, int(e.get("val_bytes", 0)), int(e.get("log2n_min", 0)),
+                           int(e.get("log2n_max", 63)), int(e.get("pass_shape", -1)),
+                           int(e.get("partitions", 0)))
+
+
+def pass_shapes(key_bytes: int, val_bytes: int) -> list[tuple[int, int]]:
+    """(threads, items per thread) of every pass shape for a key/payload width."""
+    L = load()
+    out = []
+    for s in range(L.gs_pass_shape_count()):
+        t, it = C.c_uint32(), C.c_uint32()
+        if L.gs_pass_shape_info(key_bytes, val_bytes, s, C.byref(t), C.byref(it)) != GS_OK:
+            raise GsError(GS_ERR_INVALID, "pass shape")
+        out.append((t.value, it.value))
+    return out
+
+
+def tuning_parse(text: str) -> list[dict] | None:
+    """Entries the engine reads from a tuning JSON document (None: rejected)."""
+    L = load()
+    k = L.gs_tuning_parse(text.encode(), None, 0)
+    if k < 0:
+        return None
+    arr = (gs_tuning_entry * max(1, k))()
+    assert L.gs_tuning_parse(text.encode(), arr, k) == k
+    return [{f: getattr(arr[i], f) for f, _ in gs_tuning_entry._fields_} for i in range(k)]
 
 
 def dtype_code(dt) -> int:
@@ -297,6 +364,23 @@ class Context:
     def debug_set(self, key: int, value: int):
         self._check(self.L.gs_debug_set(self.h, key, value))
 
+    def set_tuning(self, entries: list[dict]):
+        """Install a tuning table (dicts with the gs_tuning_entry fields)."""
+        arr = (gs_tuning_entry * max(1, len(entries)))()
+        for i, e in enumerate(entries):
+            arr[i] = _entry(e)
+        self._check(self.L.gs_ctx_set_tuning(self.h, arr, len(entries)))
+
+    def load_tuning(self, path):
+        self._check(self.L.gs_ctx_load_tuning(self.h, str(path).encode()))
+
+    def choice(self, key_dtype, val_bytes: int, n: int) -> tuple[int, int]:
+        """(pass shape, SampleSort buckets) the context uses for such a call."""
+        shape, parts = C.c_int(), C.c_uint32()
+        self._check(self.L.gs_ctx_choice(self.h, dtype_code(key_dtype), val_bytes, n,
+                                         C.byref(shape), C.byref(parts)))
+        return shape.value, parts.value
+
 
 class Server:
     """Serving loop on one device (gs_server_*): submit sort requests, poll
@@ -359,3 +443,56 @@ class Server:
         if st != GS_OK:
             raise GsError(st, "stats")
         return {k: getattr(s, k) for k, _ in gs_server_stats._fields_}
+
+
+# ---- per-rank binary files (gs_file_* / gs_partitions_*) ----
+
+def _raise_global(st: int):
+    if st != GS_OK:
+        raise GsError(st, load().gs_last_global_error().decode())
+
+
+def _elem_bytes(x) -> int:
+    return int(x.element_size()) if hasattr(x, "element_size") else int(x.itemsize)
+
+
+def file_count(path) -> int:
+    return int(load().gs_file_count(str(path).encode()))
+
+
+def read_file(path, out, ctx: "Context | None" = None) -> int:
+    """Read one rank file into `out` (a numpy array: host; a CUDA tensor:
+    device through `ctx`). Returns the element count read."""
+    host = isinstance(out, np.ndarray)
+    got = C.c_uint64()
+    _raise_global(load().gs_file_read(None if host else ctx.h, str(path).encode(), _ptr(out),
+                                      _count(out), _elem_bytes(out), FLAG_HOST if host else 0,
+                                      C.byref(got)))
+    return got.value
+
+
+def write_file(path, data, n: int | None = None, ctx: "Context | None" = None):
+    host = isinstance(data, np.ndarray)
+    n = _count(data) if n is None else int(n)
+    _raise_global(load().gs_file_write(None if host else ctx.h, str(path).encode(), _ptr(data), n,
+                                       _elem_bytes(data), FLAG_HOST if host else 0))
+
+
+def read_partitions(directory, nparts: int, out, ext: str = ".dat",
+                    ctx: "Context | None" = None) -> int:
+    host = isinstance(out, np.ndarray)
+    got = C.c_uint64()
+    _raise_global(load().gs_partitions_read(None if host else ctx.h, str(directory).encode(),
+                                            ext.encode(), nparts, _ptr(out), _count(out),
+                                            _elem_bytes(out), FLAG_HOST if host else 0,
+                                            C.byref(got)))
+    return got.value
+
+
+def write_partitions(directory, nparts: int, data, ext: str = ".dat", n: int | None = None,
+                     ctx: "Context | None" = None):
+    host = isinstance(data, np.ndarray)
+    n = _count(data) if n is None else int(n)
+    _raise_global(load().gs_partitions_write(None if host else ctx.h, str(directory).encode(),
+                                             ext.encode(), nparts, _ptr(data), n,
+                                             _elem_bytes(data), FLAG_HOST if host else 0))

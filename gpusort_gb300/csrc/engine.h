@@ -51,6 +51,8 @@ struct RadixJob {
 // look-back words.
 uint32_t radix_tile(int key_bytes, int val_bytes);
 int radix_num_shapes();
+// Threads per CTA and items per thread of a pass shape (false: no such shape).
+bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads, uint32_t* items);
 int radix_default_shape(int key_bytes, int val_bytes);
 // Look-back words of a 32-bit keys-only job run with the default shape.
 size_t radix_status_words_u32_shape0(uint64_t n);
@@ -76,6 +78,7 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
 
 }  // namespace gs
 struct gs_seg_plan;
+struct gs_ctx;
 namespace gs {
 std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, uint64_t n,
                            int key_bytes, uint32_t kind, bool desc, int shape);
@@ -109,6 +112,9 @@ cudaError_t launch_merge_pass(const void* in, void* out, uint64_t n, uint64_t ru
 
 // Set the message gs_last_global_error() returns on this thread.
 void set_last_global_error(const std::string& msg);
+
+// The CUDA stream a context enqueues on.
+cudaStream_t context_stream(gs_ctx* ctx);
 
 // Enqueue the whole radix pipeline on `stream`. `gen` is the context's
 // launch-generation counter (advanced once per pass launch); the caller

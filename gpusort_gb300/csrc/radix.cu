@@ -296,10 +296,40 @@ uint32_t radix_tile(int key_bytes, int val_bytes) {
 
 int radix_num_shapes() { return NUM_SHAPES; }
 
-// Measured defaults on GB300 (2^30 uniform keys): 32-bit keys run fastest
-// with 256-thread CTAs of 24 items, four per SM.
+namespace {
+template <typename K, typename V>
+void shape_info_t(int shape, uint32_t* threads, uint32_t* items) {
+  switch (shape) {
+    case 1: *threads = PassShape<K, V, 1>::THREADS; *items = PassShape<K, V, 1>::ITEMS; return;
+    case 2: *threads = PassShape<K, V, 2>::THREADS; *items = PassShape<K, V, 2>::ITEMS; return;
+    default: *threads = PassShape<K, V, 0>::THREADS; *items = PassShape<K, V, 0>::ITEMS; return;
+  }
+}
+template <typename K>
+void shape_info_k(int val_bytes, int shape, uint32_t* threads, uint32_t* items) {
+  if (val_bytes == 4) shape_info_t<K, uint32_t>(shape, threads, items);
+  else if (val_bytes == 8) shape_info_t<K, uint64_t>(shape, threads, items);
+  else shape_info_t<K, NoValue>(shape, threads, items);
+}
+}  // namespace
+
+bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads, uint32_t* items) {
+  if ((key_bytes != 4 && key_bytes != 8) || (val_bytes != 0 && val_bytes != 4 && val_bytes != 8) ||
+      shape < 0 || shape >= NUM_SHAPES)
+    return false;
+  if (key_bytes == 4) shape_info_k<uint32_t>(val_bytes, shape, threads, items);
+  else shape_info_k<uint64_t>(val_bytes, shape, threads, items);
+  return true;
+}
+
+// Measured defaults on GB300 (uniform keys, 2^22..2^30): the 512-thread
+// shape is fastest or tied for every key and value width (u32 2^30: 21.35
+// vs 21.34 ms; u64 2^29: 28.4 vs 31.5 ms; u64+u32 pairs 2^29: 41.4 vs
+// 54.7 ms; the clustered shape is slowest everywhere).
 int radix_default_shape(int key_bytes, int val_bytes) {
-  return (val_bytes == 0) ? 1 : 0;
+  (void)key_bytes;
+  (void)val_bytes;
+  return 0;
 }
 
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes) {

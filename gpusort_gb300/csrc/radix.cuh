@@ -169,19 +169,22 @@ pass_kernel(PassParams p) {
   constexpr int WARPS = Cfg::WARPS;
   constexpr int TILE = Cfg::TILE;
   constexpr bool HAS_V = Cfg::HAS_V;
-  constexpr int LB_WIN = 8;  // look-back words read per round
+  constexpr int LB_WIN = 4;         // look-back words read per round
+  constexpr int LB_SLEEP_NS = 128;  // pause after a round without progress
   using VS = typename std::conditional<HAS_V, V, uint32_t>::type;  // storage type
 
   extern __shared__ __align__(16) uint8_t s_dyn[];
-  // Stable ranking: per warp and digit, [31:0] peer mask of the current
-  // item row, [63:32] running count. After ranking, [31:0] becomes the
-  // digit's start in the tile for that warp. The unstable ranking uses the
+  // Stable ranking: per warp and digit, the peer mask of the current item
+  // row and the running count (mask in the low half for even digits, in the
+  // high half for odd ones). After ranking, [31:0] becomes the digit's start
+  // in the tile for that warp. The unstable ranking uses the
   // first RADIX+1 words as tile counters, later tile offsets.
   __shared__ __align__(16) uint64_t s_tab[WARPS][RADIX + 1];
   __shared__ uint32_t s_dst_base[RADIX];
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_seg;
+  __shared__ uint32_t s_bad;  // a digit's destination range leaves the output
   __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode
   __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
   __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
@@ -231,6 +234,7 @@ pass_kernel(PassParams p) {
   // Tiles (cluster-tiles) are claimed in launch order, so a tile only ever
   // waits on tiles held by CTAs that are already running.
   if (tid == 0 && crank == 0) s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
+  if (tid == 0) s_bad = 0;
   if ((smem_addr(&s_tab[0][0]) & 15u) == 0) {
     static_assert((WARPS * (RADIX + 1)) % 2 == 0, "s_tab is cleared in 16-byte units");
     uint4* z = reinterpret_cast<uint4*>(&s_tab[0][0]);
@@ -343,21 +347,28 @@ pass_kernel(PassParams p) {
     // Stable warp ranking: each lane sets its bit in the digit's peer mask,
     // reads back the mask and the digit's running count; the group's lowest
     // lane advances the count and clears the mask.
+    // Odd digits keep the mask in the high half and the count in the low
+    // half, so the lanes' atomics spread over all 32 banks.
     const uint32_t lt = lanemask_lt();
     const uint32_t bit = 1u << lane;
     uint64_t* tab = s_tab[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
       const uint32_t d = (wloc + 32 * i < tile_n) ? digit_at(i) : uint32_t(RADIX);
-      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]), bit);
+      const uint32_t odd = d & 1u;
+      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]) + odd, bit);
       __syncwarp();
       const uint64_t e = tab[d];
       __syncwarp();
-      const uint32_t peers = uint32_t(e);
+      const uint32_t lo = uint32_t(e), hi = uint32_t(e >> 32);
+      const uint32_t peers = odd ? hi : lo;
+      const uint32_t base = odd ? lo : hi;
       const uint32_t below = peers & lt;
-      const uint32_t base = uint32_t(e >> 32);
       set_rank(i, base + __popc(below));
-      if (below == 0) tab[d] = uint64_t(base + __popc(peers)) << 32;
+      if (below == 0) {
+        const uint64_t c = base + __popc(peers);
+        tab[d] = odd ? c : (c << 32);
+      }
       __syncwarp();
     }
   }
@@ -372,7 +383,8 @@ pass_kernel(PassParams p) {
       uint32_t run = 0;
 #pragma unroll
       for (int w = 0; w < WARPS; ++w) {
-        const uint32_t c = uint32_t(s_tab[w][tid] >> 32);
+        const uint64_t e = s_tab[w][tid];
+        const uint32_t c = (tid & 1) ? uint32_t(e) : uint32_t(e >> 32);
         s_tab[w][tid] = run;  // this thread owns column tid
         run += c;
       }
@@ -405,18 +417,23 @@ pass_kernel(PassParams p) {
 
   // Decoupled look-back over preceding units, LB_WIN words per round,
   // bounded by spin_limit rounds without progress (the cluster's first CTA).
+  // While the nearest word is pending, one word is polled per round after a
+  // short sleep, so waiting warps leave issue slots and L1 bandwidth to the
+  // tiles they wait for.
   uint32_t prefix = 0;
   if (tid < RADIX && leader) {
     if (ctile > first_unit) {
       int64_t t = int64_t(ctile) - 1;
       uint32_t idle_rounds = 0;
       const bool stall = p.inject_stall && ctile == 1;
+      int win = LB_WIN;
       while (true) {
         uint64_t w[LB_WIN];
 #pragma unroll
         for (int k = 0; k < LB_WIN; ++k) {
           const int64_t tt = t - k;
-          w[k] = (tt >= 0 && !stall) ? ld_relaxed(p.status + uint64_t(tt) * RADIX + tid) : 0ull;
+          w[k] = (k < win && tt >= 0 && !stall) ? ld_relaxed(p.status + uint64_t(tt) * RADIX + tid)
+                                                : 0ull;
         }
         int consumed = 0;
         bool done = false;
@@ -432,9 +449,15 @@ pass_kernel(PassParams p) {
         }
         if (done) break;
         t -= consumed;
-        if (consumed == 0 && ++idle_rounds > p.spin_limit) {
-          atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
-          break;
+        if (consumed == 0) {
+          if (++idle_rounds > p.spin_limit) {
+            atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
+            break;
+          }
+          __nanosleep(LB_SLEEP_NS);
+          win = 1;
+        } else {
+          win = LB_WIN;
         }
       }
       st_relaxed(status + tid, make_status(FLAG_INC, gen, prefix + unit_count));
@@ -451,6 +474,12 @@ pass_kernel(PassParams p) {
                             ? p.seg_binbase[(size_t(seg) * p.seg_digits + p.pass) * RADIX + tid]
                             : plan.binbase[p.pass][tid];
     s_dst_base[tid] = uint32_t(e0) + bb + prefix + cl_excl - tile_excl;
+    // This CTA writes the digit's elements to [e0 + bb + prefix + cl_excl,
+    // + count): the range is checked once per digit, not per element.
+    if (count != 0 && uint64_t(e0) + bb + prefix + cl_excl + count > e1) {
+      s_bad = 1;
+      atomicOr(p.err, ERR_SCATTER_RANGE);
+    }
     if (unstable) {
       s_cnt[tid] = tile_excl;
     } else {
@@ -478,11 +507,11 @@ pass_kernel(PassParams p) {
 
   // Scatter: consecutive tile positions of one digit go to consecutive
   // output addresses.
-  const uint32_t n32 = uint32_t(e1);  // end of the segment (n < 2^32)
+  const uint32_t n_ok = s_bad ? 0u : tile_n;  // a tile that failed the check writes nothing
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     const uint32_t r = uint32_t(i) * THREADS + tid;
-    if (r < tile_n) {
+    if (r < n_ok) {
       const K k = s_keys[r];
       uint32_t d;
       VS v;
@@ -493,12 +522,8 @@ pass_kernel(PassParams p) {
         d = key_digit(k);
       }
       const uint32_t dst = s_dst_base[d] + r;
-      if (dst < n32) {
-        dst_k[dst] = last ? kx.inv(k) : k;
-        if constexpr (HAS_V) dst_v[dst] = v;
-      } else {
-        atomicOr(p.err, ERR_SCATTER_RANGE);
-      }
+      dst_k[dst] = last ? kx.inv(k) : k;
+      if constexpr (HAS_V) dst_v[dst] = v;
     }
   }
   if constexpr (CLUSTER > 1) cluster_wait();

@@ -97,15 +97,15 @@ group_sort_kernel(GroupSortParams p) {
     uint32_t rank2[ITEMS / 2];
 #pragma unroll
     for (int i = 0; i < ITEMS / 2; ++i) rank2[i] = 0;
-    auto digit_at = [&](int i) -> uint32_t {
-      return sid_pass ? uint32_t(s_sid[cur][wloc + 32 * i])
-                      : (uint32_t(keys[i] >> shift) & (RADIX - 1));
-    };
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
       const uint32_t l = wloc + 32 * i;
       keys[i] = l < cnt ? s_key[cur][l] : K(0);
     }
+    auto digit_at = [&](int i) -> uint32_t {
+      return sid_pass ? uint32_t(s_sid[cur][wloc + 32 * i])
+                      : (uint32_t(keys[i] >> shift) & (RADIX - 1));
+    };
     uint64_t* tab = s_tab[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {

@@ -100,6 +100,15 @@ inline gs_ctx* Context(int device) {
   if (it != ctxs.end()) return it->second;
   gs_ctx* c = gs_ctx_create(device, 0);
   if (!c) throw ThrustException(gs_last_global_error());
+  // An autotuner table (python -m gpusort_gb300.autotune) named by
+  // GPUSORT_GB300_TUNING applies to every context of the process.
+  if (const char* path = std::getenv("GPUSORT_GB300_TUNING")) {
+    if (gs_ctx_load_tuning(c, path) != GS_OK) {
+      const std::string msg = gs_last_error(c);
+      gs_ctx_destroy(c);
+      throw ThrustException(msg.c_str());
+    }
+  }
   ctxs[device] = c;
   return c;
 }

@@ -214,6 +214,42 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
                                     UINT64_MAX: per-type default */
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
+/* ---- Tuning table (autotuner output) ----
+ * No counterpart in the reference, whose algorithm parameters are
+ * hard-coded (include/helpers/hyksort_helper.h:343-344,
+ * include/helpers/samplesort_helper.h:429, src/cuda_utils.cu:515). The
+ * engine's radix digit is fixed at 8 bits; what a table chooses per key
+ * type, payload width and size is the pass kernel's tile shape (threads x
+ * items per thread) and the SampleSort bucket count. gpusort_gb300.autotune
+ * measures them on the device and writes the JSON file that
+ * gs_ctx_load_tuning reads. An explicit GS_DEBUG_PASS_SHAPE or
+ * gs_opts.partitions still wins over the table. */
+typedef struct gs_tuning_entry {
+  int32_t key_dtype;      /* gs_dtype */
+  int32_t val_bytes;      /* payload bytes: 0 (keys only), 4 or 8 */
+  uint32_t log2n_min;     /* applies when floor(log2(n)) is in [min, max] */
+  uint32_t log2n_max;
+  int32_t pass_shape;     /* radix pass tile shape, -1: engine default */
+  uint32_t partitions;    /* SampleSort buckets when gs_opts leaves 0; 0: default */
+} gs_tuning_entry;
+/* Number of pass tile shapes and the threads / items per thread of one. */
+int gs_pass_shape_count(void);
+gs_status gs_pass_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads,
+                             uint32_t* items_per_thread);
+/* Replace the context's table (count 0 clears it); the first matching
+ * entry wins. */
+gs_status gs_ctx_set_tuning(gs_ctx* ctx, const gs_tuning_entry* entries, uint32_t count);
+/* Parse a tuning JSON document: {"entries": [{"key_dtype": "u32" | 0..5,
+ * "val_bytes": .., "log2n_min": .., "log2n_max": .., "pass_shape": ..,
+ * "partitions": ..}, ...]} (other keys are ignored). Returns the number of
+ * entries (all written when <= capacity), or -1 on a syntax error. */
+int gs_tuning_parse(const char* json, gs_tuning_entry* out, uint32_t capacity);
+/* Read and apply a tuning JSON file. */
+gs_status gs_ctx_load_tuning(gs_ctx* ctx, const char* path);
+/* The pass shape and SampleSort bucket count the context uses for a call. */
+gs_status gs_ctx_choice(gs_ctx* ctx, gs_dtype key_dtype, int val_bytes, uint64_t n,
+                        int* pass_shape, uint32_t* partitions);
+
 /* Sort 32-bit keys (GS_U32, GS_I32, GS_F32) in device memory WITHOUT
  * ALLOCATING. No counterpart in the reference: it exists for callers that
  * cannot call cudaMalloc - code running under a framework whose caching
@@ -234,6 +270,36 @@ gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 #define GS_NOALLOC_MAX_KEYS (1ull << 20)
 gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out,
                                uint64_t n, uint32_t flags, void* stream);
+
+/* ---- Per-rank binary files ----
+ * The reference's test driver keeps one file per MPI rank, <dir>/<rank><ext>
+ * (".dat" by default), holding a native int64 element count followed by the
+ * raw elements (src/test/utils.h:610-661: GetFilePath, ReadData, SaveData,
+ * SaveMyData; src/test/ifstream.h:38-73, src/test/ofstream.h:34-64). Here
+ * the p rank files of a job are the p partitions of one array.
+ * - By default `dst` / `src` are device memory of the context's device and
+ *   the data streams through pinned staging buffers on the context's stream
+ *   (the call returns when the data has landed); with GS_FLAG_HOST they are
+ *   host memory and `ctx` may be NULL.
+ * - gs_partitions_write splits n elements over nparts files with the
+ *   reference's block size (include/common.h:146-155) and gives the last file
+ *   the remainder. (The reference's SaveData writes the block size for every
+ *   rank and so drops the tail when the last block is the larger one, e.g.
+ *   9 elements over 4 ranks; files it does write read back identically.)
+ * - Errors are described by gs_last_global_error(). */
+int64_t gs_file_count(const char* path);  /* element count, -1 if unreadable */
+gs_status gs_file_read(gs_ctx* ctx, const char* path, void* dst, uint64_t capacity,
+                       uint32_t elem_bytes, uint32_t flags, uint64_t* n_read);
+gs_status gs_file_write(gs_ctx* ctx, const char* path, const void* src, uint64_t n,
+                        uint32_t elem_bytes, uint32_t flags);
+gs_status gs_partitions_read(gs_ctx* ctx, const char* dir, const char* ext, int nparts,
+                             void* dst, uint64_t capacity, uint32_t elem_bytes,
+                             uint32_t flags, uint64_t* n_total);
+gs_status gs_partitions_write(gs_ctx* ctx, const char* dir, const char* ext, int nparts,
+                              const void* src, uint64_t n, uint32_t elem_bytes,
+                              uint32_t flags);
+/* Elements in each of the first nparts-1 files of gs_partitions_write. */
+uint64_t gs_partition_block(uint64_t n, int nparts);
 
 /* ---- Serving loop (continuous batching) ----
  * No counterpart in the reference (its callers sort one array per call,
