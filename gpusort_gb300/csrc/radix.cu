@@ -69,17 +69,17 @@ template <typename K, typename V, int S> struct PassShape;
 // selectable for tuning. Key/value sorts never use clusters: a clustered
 // 256-thread pair variant raised an illegal-instruction fault on GB300
 // whose cause is not yet understood.
-template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 16, 2, 1> {};
+template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 24, 2, 1> {};
 template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 20, 4, 1> {};
 template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 16, 2, 8> {};
-template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 12, 2, 1> {};
+template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 14, 2, 1> {};
 template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4, 1> {};
 template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 12, 2, 8> {};
-template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 12, 2, 1> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 14, 2, 1> {};
 template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4, 1> {};
 template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 10, 4, 1> {};
 template <typename K, typename V, int S>
-struct PassShape : Shape<(S == 0 ? 512 : 256), (S == 0 ? 8 : 6), (S == 0 ? 2 : 4), 1> {};
+struct PassShape : Shape<(S == 0 ? 512 : 256), (S == 0 ? 10 : 6), (S == 0 ? 2 : 4), 1> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 1024;  // no shape has a smaller tile (smallest: 256 x 6)
 
@@ -323,9 +323,11 @@ bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads
 }
 
 // Measured defaults on GB300 (uniform keys, 2^22..2^30): the 512-thread
-// shape is fastest or tied for every key and value width (u32 2^30: 21.35
-// vs 21.34 ms; u64 2^29: 28.4 vs 31.5 ms; u64+u32 pairs 2^29: 41.4 vs
-// 54.7 ms; the clustered shape is slowest everywhere).
+// shape is fastest for every key and value width; its items per thread are
+// the most that fit 64 registers without spilling (u32 keys 512 x 24: 2^29
+// in 9.40 ms vs 10.71 at 16 items; u64 keys 512 x 14: 26.99 vs 28.57 ms at
+// 12; u64 + u32 pairs 512 x 10: 37.7 vs 41.7 ms at 8). The clustered shape
+// is slowest everywhere.
 int radix_default_shape(int key_bytes, int val_bytes) {
   (void)key_bytes;
   (void)val_bytes;
