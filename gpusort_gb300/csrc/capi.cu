@@ -327,6 +327,59 @@ gs_status check_err_word(gs_ctx* ctx) {
   return GS_OK;
 }
 
+// Copy kernel for transfers between device memory and pinned host memory
+// that the device addresses directly (cudaHostAlloc, cudaHostRegister): the
+// SMs load and store across the CPU-GPU link. Four independent 16-byte
+// loads per thread keep enough requests in flight for the link's latency.
+__global__ void __launch_bounds__(512) link_copy_kernel(const uint8_t* __restrict__ src,
+                                                        uint8_t* __restrict__ dst,
+                                                        uint64_t bytes) {
+  const uint64_t n16 = bytes / 16;
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+    d[i] = a;
+    d[i + stride] = b;
+    d[i + 2 * stride] = c;
+    d[i + 3 * stride] = e;
+  }
+  for (; i < n16; i += stride) d[i] = s[i];
+  if (blockIdx.x == 0 && threadIdx.x < (bytes & 15u)) dst[n16 * 16 + threadIdx.x] = src[n16 * 16 + threadIdx.x];
+}
+
+// The device address of pinned, device-mapped host memory, or null.
+const void* mapped_host(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host <-> device transfer on the context's stream. Pinned host memory the
+// device can address, with both ends 16-byte aligned, moves through the SMs:
+// on GB300 that sustained about 200 GB/s each way, while the copy engine
+// gave between 56 and 200 GB/s for the same buffers. Everything else goes
+// through cudaMemcpyAsync.
+cudaError_t link_copy(gs_ctx* ctx, void* dst, const void* src, uint64_t bytes, bool to_device) {
+  if (bytes == 0) return cudaSuccess;
+  const void* host = to_device ? src : dst;
+  const void* mapped = mapped_host(host);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
+  if (!mapped || !aligned)
+    return cudaMemcpyAsync(dst, src, bytes,
+                           to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, ctx->stream);
+  const uint8_t* s = static_cast<const uint8_t*>(to_device ? mapped : src);
+  uint8_t* d = static_cast<uint8_t*>(to_device ? dst : const_cast<void*>(mapped));
+  const unsigned blocks = unsigned(std::max(1, ctx->props.num_sms) * 2);
+  link_copy_kernel<<<blocks, 512, 0, ctx->stream>>>(s, d, bytes);
+  return cudaGetLastError();
+}
+
 // Device-memory radix sort of keys or pairs.
 gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind,
                       const void* kin, const void* vin, void* kout, void* vout,
@@ -526,18 +579,16 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
       if (st != GS_OK) return st;
     }
     if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
-    e = cudaMemcpyAsync(ctx->stage_k.ptr, kin, size_t(n) * kb, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess && has_v)
-      e = cudaMemcpyAsync(ctx->stage_v.ptr, vin, size_t(n) * vb, cudaMemcpyHostToDevice, ctx->stream);
+    e = link_copy(ctx, ctx->stage_k.ptr, kin, uint64_t(n) * kb, true);
+    if (e == cudaSuccess && has_v) e = link_copy(ctx, ctx->stage_v.ptr, vin, uint64_t(n) * vb, true);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "host to device copy");
     if (ctx->timing) { ctx->n_phases = 0; phase_mark(ctx, "Transfer in"); }
     st = dispatch_sort(ctx, kb, kk, vb, vk, ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr,
                        ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr, n, flags, opts);
     if (st != GS_OK) return st;
     phase_mark(ctx, "Local sort");
-    e = cudaMemcpyAsync(kout, ctx->stage_k.ptr, size_t(n) * kb, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess && has_v)
-      e = cudaMemcpyAsync(vout, ctx->stage_v.ptr, size_t(n) * vb, cudaMemcpyDeviceToHost, ctx->stream);
+    e = link_copy(ctx, kout, ctx->stage_k.ptr, uint64_t(n) * kb, false);
+    if (e == cudaSuccess && has_v) e = link_copy(ctx, vout, ctx->stage_v.ptr, uint64_t(n) * vb, false);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "device to host copy");
     phase_mark(ctx, "Transfer out");
     return check_err_word(ctx);
