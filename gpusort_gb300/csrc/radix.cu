@@ -56,6 +56,8 @@ namespace {
 
 constexpr int UPSWEEP_THREADS = 512;
 constexpr int UPSWEEP_UNROLL = 8;
+constexpr uint32_t UPSWEEP_SMEM = 64u << 10;  // column-spread histograms per CTA
+constexpr int UPSWEEP_PER_SM = 3;
 
 // Tile shapes of the pass kernel (threads per block, items per thread,
 // blocks per SM), selectable per call; shape 0 is the default. Larger
@@ -179,13 +181,25 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   up.desc = job.desc;
   up.val_digits = vd;
   up.work = job.work;
+  // Histogram columns: as many (up to 32) as fit UPSWEEP_SMEM bytes.
+  const uint32_t total_digits = vd + uint32_t(sizeof(K));
+  uint32_t cl = 0;
+  while (cl < 5 && ((total_digits * RADIX) << (cl + 1)) * 4u <= UPSWEEP_SMEM) ++cl;
+  up.col_log2 = cl;
+  const size_t usmem = size_t((total_digits * RADIX) << cl) * 4u;
+  static bool uattr = false;
+  auto ukern = upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL>;
+  if (!uattr) {
+    e = cudaFuncSetAttribute(ukern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(UPSWEEP_SMEM));
+    if (e != cudaSuccess) return e;
+    uattr = true;
+  }
   const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
   uint64_t ublocks = (job.n + chunk - 1) / chunk;
-  const uint64_t umax = uint64_t(props.num_sms) * 4;
+  const uint64_t umax = uint64_t(props.num_sms) * UPSWEEP_PER_SM;
   if (ublocks > umax) ublocks = umax;
   if (ublocks == 0) ublocks = 1;
-  upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL>
-      <<<unsigned(ublocks), UPSWEEP_THREADS, 0, stream>>>(up);
+  ukern<<<unsigned(ublocks), UPSWEEP_THREADS, usmem, stream>>>(up);
   if (job.marks) cudaEventRecord(job.marks[1], stream);
 
   PlanParams pp{};
