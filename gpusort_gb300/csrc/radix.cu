@@ -181,18 +181,19 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   up.desc = job.desc;
   up.val_digits = vd;
   up.work = job.work;
-  // Histogram columns: as many (up to 32) as fit UPSWEEP_SMEM bytes.
+  // Histogram columns: as many (4 to 16) as fit UPSWEEP_SMEM bytes.
   const uint32_t total_digits = vd + uint32_t(sizeof(K));
-  uint32_t cl = 0;
-  while (cl < 5 && ((total_digits * RADIX) << (cl + 1)) * 4u <= UPSWEEP_SMEM) ++cl;
-  up.col_log2 = cl;
+  uint32_t cl = 2;
+  while (cl < 4 && ((total_digits * RADIX) << (cl + 1)) * 4u <= UPSWEEP_SMEM) ++cl;
   const size_t usmem = size_t((total_digits * RADIX) << cl) * 4u;
-  static bool uattr = false;
-  auto ukern = upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL>;
-  if (!uattr) {
+  auto ukern = cl == 4 ? upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 4>
+             : cl == 3 ? upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 3>
+                       : upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 2>;
+  static bool uattr[5] = {false, false, false, false, false};
+  if (!uattr[cl]) {
     e = cudaFuncSetAttribute(ukern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(UPSWEEP_SMEM));
     if (e != cudaSuccess) return e;
-    uattr = true;
+    uattr[cl] = true;
   }
   const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
   uint64_t ublocks = (job.n + chunk - 1) / chunk;

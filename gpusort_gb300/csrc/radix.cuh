@@ -32,74 +32,92 @@ namespace gs {
 // ---------------------------------------------------------------------------
 
 // The histograms live in shared memory as hist[digit][bin][column], with
-// 2^col_log2 columns and lane l counting into column l mod 2^col_log2: lanes
-// of a warp that draw the same bank for different bins then mostly land in
-// different banks, so the random-bin atomics of a warp take about 1.5
-// shared-memory wavefronts instead of 3.5 (16 columns). Atomics to one
-// address from a whole warp are combined in hardware, so skewed inputs need
-// no special case.
-template <typename K, typename V, int THREADS, int UNROLL>
+// 2^CL columns and lane l counting into column l mod 2^CL: lanes of a warp
+// that draw the same bank for different bins then mostly land in different
+// banks, so the random-bin atomics of a warp take about 2 shared-memory
+// wavefronts instead of 3.5 (16 columns). CL is a compile-time constant so
+// each counter's address is one shift-add. Atomics to one address from a
+// whole warp are combined in hardware, so skewed inputs need no special
+// case.
+template <typename K, typename V, int THREADS, int UNROLL, int CL>
 __global__ void __launch_bounds__(THREADS)
 upsweep_kernel(UpsweepParams p) {
   constexpr int KD = Bits<K>::DIGITS;
   constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
-  extern __shared__ __align__(16) uint32_t s_hist[];  // [digits][RADIX][columns]
+  constexpr uint32_t NC = 1u << CL;  // columns per bin
+  extern __shared__ __align__(16) uint32_t s_hist[];  // [digits][RADIX][NC]
   const uint32_t vd = p.val_digits;
   const uint32_t total_digits = vd + KD;
-  const uint32_t cl = p.col_log2;
-  const uint32_t words = (total_digits * RADIX) << cl;
+  const uint32_t words = total_digits * RADIX * NC;
   for (uint32_t i = threadIdx.x; i < words; i += THREADS) s_hist[i] = 0;
   __syncthreads();
-  const uint32_t col = threadIdx.x & ((1u << cl) - 1);
-  auto add = [&](uint32_t digit, uint32_t bin, bool valid) {
-    if (valid) atomicAdd(&s_hist[((digit * RADIX + bin) << cl) + col], 1u);
-  };
+  // This thread's column; digit q's histogram starts at q * RADIX * NC.
+  uint32_t* const hk = s_hist + vd * RADIX * NC + (threadIdx.x & (NC - 1));
+  uint32_t* const hv = s_hist + (threadIdx.x & (NC - 1));
 
   const K* keys = static_cast<const K*>(p.keys);
+  const V* vals = nullptr;
+  if constexpr (HAS_V) vals = static_cast<const V*>(p.vals);
   const bool desc = p.desc != 0;
   const uint64_t n = p.n;
   const uint64_t chunk = uint64_t(THREADS) * UNROLL;
-  for (uint64_t base = uint64_t(blockIdx.x) * chunk; base < n;
-       base += uint64_t(gridDim.x) * chunk) {
-    K k[UNROLL];
-    bool valid[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
-      valid[u] = idx < n;
-      k[u] = valid[u] ? ld_stream(keys + idx) : K(0);
-    }
+  auto count = [&](const K (&k)[UNROLL], const bool (&valid)[UNROLL]) {
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       const K b = order_bits<K>(k[u], p.key_kind, desc);
 #pragma unroll
-      for (int d = 0; d < KD; ++d)
-        add(vd + d, uint32_t(b >> (RADIX_BITS * d)) & (RADIX - 1), valid[u]);
+      for (int d = 0; d < KD; ++d) {
+        const uint32_t bin = uint32_t(b >> (RADIX_BITS * d)) & (RADIX - 1);
+        if (valid[u]) atomicAdd(hk + d * RADIX * NC + (bin << CL), 1u);
+      }
     }
+  };
+  auto count_vals = [&](uint64_t base, const bool (&valid)[UNROLL]) {
     if constexpr (HAS_V) {
-      if (vd > 0) {
-        const V* vals = static_cast<const V*>(p.vals);
-        V v[UNROLL];
+      V v[UNROLL];
 #pragma unroll
-        for (int u = 0; u < UNROLL; ++u) {
-          const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
-          v[u] = valid[u] ? ld_stream(vals + idx) : V(0);
-        }
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
+        v[u] = valid[u] ? ld_stream(vals + idx) : V(0);
+      }
 #pragma unroll
-        for (int u = 0; u < UNROLL; ++u) {
-          const V b = order_bits<V>(v[u], p.val_kind, desc);
+      for (int u = 0; u < UNROLL; ++u) {
+        const V b = order_bits<V>(v[u], p.val_kind, desc);
 #pragma unroll
-          for (int d = 0; d < Bits<V>::DIGITS; ++d)
-            add(d, uint32_t(b >> (RADIX_BITS * d)) & (RADIX - 1), valid[u]);
+        for (int d = 0; d < Bits<V>::DIGITS; ++d) {
+          const uint32_t bin = uint32_t(b >> (RADIX_BITS * d)) & (RADIX - 1);
+          if (valid[u]) atomicAdd(hv + d * RADIX * NC + (bin << CL), 1u);
         }
       }
     }
+  };
+  for (uint64_t base = uint64_t(blockIdx.x) * chunk; base < n;
+       base += uint64_t(gridDim.x) * chunk) {
+    K k[UNROLL];
+    bool valid[UNROLL];
+    if (base + chunk <= n) {  // interior chunk: no bounds checks
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        valid[u] = true;
+        k[u] = ld_stream(keys + base + uint64_t(u) * THREADS + threadIdx.x);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
+        valid[u] = idx < n;
+        k[u] = valid[u] ? ld_stream(keys + idx) : K(0);
+      }
+    }
+    count(k, valid);
+    if (HAS_V && vd > 0) count_vals(base, valid);
   }
   __syncthreads();
   uint32_t* g = &p.work->hist[0][0];
   for (uint32_t i = threadIdx.x; i < total_digits * RADIX; i += THREADS) {
     uint32_t c = 0;
-    for (uint32_t j = 0; j < (1u << cl); ++j) c += s_hist[(i << cl) + ((j + i) & ((1u << cl) - 1))];
+#pragma unroll
+    for (uint32_t j = 0; j < NC; ++j) c += s_hist[i * NC + ((j + i) & (NC - 1))];
     if (c) atomicAdd(&g[i], c);
   }
 }

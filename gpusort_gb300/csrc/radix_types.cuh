@@ -28,7 +28,6 @@ struct UpsweepParams {
   uint32_t key_kind, val_kind;
   uint32_t desc;
   uint32_t val_digits;    // 0, or the value's digit count (ties by value)
-  uint32_t col_log2;      // histogram columns per bin: 2^col_log2
   SortWork* work;
 };
 
