@@ -380,10 +380,17 @@ cudaError_t link_copy(gs_ctx* ctx, void* dst, const void* src, uint64_t bytes, b
   return cudaGetLastError();
 }
 
+// Device copies the upsweep makes of a host call's pinned input, which it
+// reads directly across the CPU-GPU link (see sort_common).
+struct HostFuse {
+  void* keys_copy = nullptr;
+  void* vals_copy = nullptr;
+};
+
 // Device-memory radix sort of keys or pairs.
 gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind,
                       const void* kin, const void* vin, void* kout, void* vout,
-                      uint64_t n, uint32_t flags) {
+                      uint64_t n, uint32_t flags, const HostFuse* fuse = nullptr) {
   const bool desc = flags & GS_FLAG_DESCENDING;
   const bool stable = flags & GS_FLAG_PAIRS_STABLE;
   gs::RadixJob job;
@@ -405,6 +412,10 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
   job.spin_limit = ctx->spin_limit;
   job.inject_stall = ctx->inject_stall;
   job.shape = pass_shape_for(ctx, kb, kkind, vb, n);
+  if (fuse) {
+    job.keys_copy = fuse->keys_copy;
+    job.vals_copy = fuse->vals_copy;
+  }
   ctx->inject_stall = 0;
 
   gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
@@ -577,6 +588,30 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
     if (has_v) {
       st = ensure(ctx, ctx->stage_v, size_t(n) * vb);
       if (st != GS_OK) return st;
+    }
+    // Pinned host input on the radix path: the upsweep reads it across the
+    // CPU-GPU link once and keeps a device copy for the passes, so the
+    // transfer in overlaps the histogram kernel. (Writing the last pass's
+    // scatter straight into pinned host output measured slower on GB300
+    // than sorting in HBM and copying out: 70.6 vs 61.0 ms for 2^30 keys.)
+    const uint32_t algo = opts ? opts->algo : GS_ALGO_AUTO;
+    const bool radix_path = has_v || n < 4096 || (algo != GS_ALGO_SAMPLE && algo != GS_ALGO_HYK);
+    const void* mk = mapped_host(kin);
+    const void* mv = has_v ? mapped_host(vin) : nullptr;
+    if (radix_path && mk && (!has_v || mv)) {
+      HostFuse fu;
+      fu.keys_copy = ctx->stage_k.ptr;
+      fu.vals_copy = has_v ? ctx->stage_v.ptr : nullptr;
+      if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
+      st = device_sort(ctx, kb, kk, vb, vk, mk, mv, ctx->stage_k.ptr,
+                       has_v ? ctx->stage_v.ptr : nullptr, n, flags, &fu);
+      if (st != GS_OK) return st;
+      phase_mark(ctx, "Local sort");
+      e = link_copy(ctx, kout, ctx->stage_k.ptr, uint64_t(n) * kb, false);
+      if (e == cudaSuccess && has_v) e = link_copy(ctx, vout, ctx->stage_v.ptr, uint64_t(n) * vb, false);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "device to host copy");
+      phase_mark(ctx, "Transfer out");
+      return check_err_word(ctx);
     }
     if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
     e = link_copy(ctx, ctx->stage_k.ptr, kin, uint64_t(n) * kb, true);

@@ -45,6 +45,11 @@ struct RadixJob {
   cudaEvent_t* marks = nullptr;
   int shape = 0;                    // pass-kernel tile shape (0 .. radix_num_shapes()-1)
   uint32_t* gen_counter = nullptr;  // look-back tag counter of `status` (default: in work)
+  // Optional: the upsweep copies keys_in / vals_in (e.g. pinned host memory
+  // the device reads directly) to these device buffers and the passes read
+  // the copies, so the input crosses the CPU-GPU link once.
+  void* keys_copy = nullptr;
+  void* vals_copy = nullptr;
 };
 
 // Smallest tile (elements) of the pass kernel over all shapes: sizes the

@@ -175,6 +175,8 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   UpsweepParams up{};
   up.keys = job.keys_in;
   up.vals = job.vals_in;
+  up.copy_keys = job.keys_copy;
+  up.copy_vals = HAS_V ? job.vals_copy : nullptr;
   up.n = job.n;
   up.key_kind = job.key_kind;
   up.val_kind = job.val_kind;
@@ -203,17 +205,23 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   ukern<<<unsigned(ublocks), UPSWEEP_THREADS, usmem, stream>>>(up);
   if (job.marks) cudaEventRecord(job.marks[1], stream);
 
+  // With copies, the passes read the copies.
+  RadixJob pj = job;
+  if (job.keys_copy) {
+    pj.keys_in = job.keys_copy;
+    if (HAS_V) pj.vals_in = job.vals_copy;
+  }
   PlanParams pp{};
   pp.work = job.work;
   pp.n = job.n;
   pp.digits = digits;
-  pp.in_place = (job.keys_in == job.keys_out) ||
-                (HAS_V && job.vals_in == job.vals_out);
+  pp.in_place = (pj.keys_in == pj.keys_out) ||
+                (HAS_V && pj.vals_in == pj.vals_out);
   pp.reverse_first = job.reverse_first;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
   plan_kernel<<<1, 256, 0, stream>>>(pp);
   if (job.marks) cudaEventRecord(job.marks[2], stream);
-  return launch_passes<K, V, S>(job, nullptr, digits, vd, props, gen, stream);
+  return launch_passes<K, V, S>(pj, nullptr, digits, vd, props, gen, stream);
 }
 
 }  // namespace

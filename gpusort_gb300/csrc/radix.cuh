@@ -27,6 +27,32 @@
 
 namespace gs {
 
+// Branch-free order transform of one element type: forward maps raw bits
+// to bits whose unsigned order is the requested order (std::less, or
+// std::greater when `desc`; include/common.h:156-164 maps the comparator to
+// that flag); inverse undoes it. Signed keys flip the sign bit; IEEE keys
+// flip every bit of negative values and only the sign bit of the others,
+// so -inf < ... < -0 < +0 < ... < +inf.
+template <typename U>
+struct OrderXform {
+  U fmask, smask, dmask;
+  __device__ __forceinline__ OrderXform(uint32_t kind, bool desc)
+      : fmask(kind == KIND_FLOAT ? ~U(0) : U(0)),
+        smask(kind == KIND_UNSIGNED ? U(0) : Bits<U>::SIGN),
+        dmask(desc ? ~U(0) : U(0)) {}
+  __device__ __forceinline__ U fwd(U x) const {
+    using S = typename std::make_signed<U>::type;
+    const U neg = U(S(x) >> (8 * sizeof(U) - 1));
+    return x ^ ((neg & fmask) | smask) ^ dmask;
+  }
+  __device__ __forceinline__ U inv(U y) const {
+    using S = typename std::make_signed<U>::type;
+    const U t = y ^ dmask;
+    const U was_neg = U(S(~t) >> (8 * sizeof(U) - 1));
+    return t ^ ((was_neg & fmask) | smask);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Upsweep: all digit histograms in one read.
 // ---------------------------------------------------------------------------
@@ -61,6 +87,9 @@ upsweep_kernel(UpsweepParams p) {
   const bool desc = p.desc != 0;
   const uint64_t n = p.n;
   const uint64_t chunk = uint64_t(THREADS) * UNROLL;
+  K* const copy_k = static_cast<K*>(p.copy_keys);
+  V* copy_v = nullptr;
+  if constexpr (HAS_V) copy_v = static_cast<V*>(p.copy_vals);
   auto count = [&](const K (&k)[UNROLL], const bool (&valid)[UNROLL]) {
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
@@ -79,7 +108,9 @@ upsweep_kernel(UpsweepParams p) {
       for (int u = 0; u < UNROLL; ++u) {
         const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
         v[u] = valid[u] ? ld_stream(vals + idx) : V(0);
+        if (copy_v && valid[u]) copy_v[idx] = v[u];
       }
+      if (vd == 0) return;  // values only copied
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const V b = order_bits<V>(v[u], p.val_kind, desc);
@@ -109,8 +140,15 @@ upsweep_kernel(UpsweepParams p) {
         k[u] = valid[u] ? ld_stream(keys + idx) : K(0);
       }
     }
+    if (copy_k) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u)
+        if (valid[u]) copy_k[base + uint64_t(u) * THREADS + threadIdx.x] = k[u];
+    }
     count(k, valid);
-    if (HAS_V && vd > 0) count_vals(base, valid);
+    if constexpr (HAS_V) {
+      if (vd > 0 || copy_v) count_vals(base, valid);
+    }
   }
   __syncthreads();
   uint32_t* g = &p.work->hist[0][0];
@@ -137,27 +175,6 @@ struct PassConfig {
   static constexpr size_t DYN_SMEM = SMEM_KEYS + SMEM_VALS;
 };
 
-// Branch-free order transform of one element type: forward maps raw bits
-// to bits whose unsigned order is the requested order; inverse undoes it.
-template <typename U>
-struct OrderXform {
-  U fmask, smask, dmask;
-  __device__ __forceinline__ OrderXform(uint32_t kind, bool desc)
-      : fmask(kind == KIND_FLOAT ? ~U(0) : U(0)),
-        smask(kind == KIND_UNSIGNED ? U(0) : Bits<U>::SIGN),
-        dmask(desc ? ~U(0) : U(0)) {}
-  __device__ __forceinline__ U fwd(U x) const {
-    using S = typename std::make_signed<U>::type;
-    const U neg = U(S(x) >> (8 * sizeof(U) - 1));
-    return x ^ ((neg & fmask) | smask) ^ dmask;
-  }
-  __device__ __forceinline__ U inv(U y) const {
-    using S = typename std::make_signed<U>::type;
-    const U t = y ^ dmask;
-    const U was_neg = U(S(~t) >> (8 * sizeof(U) - 1));
-    return t ^ ((was_neg & fmask) | smask);
-  }
-};
 
 // Keys live in the transformed domain between passes: the first pass that
 // runs transforms them on load, the last one restores raw bits on store.

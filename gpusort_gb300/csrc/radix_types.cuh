@@ -29,6 +29,8 @@ struct UpsweepParams {
   uint32_t desc;
   uint32_t val_digits;    // 0, or the value's digit count (ties by value)
   SortWork* work;
+  void* copy_keys;        // when set: every key read is also stored here
+  void* copy_vals;        // (and every value, when val_digits > 0)
 };
 
 struct PlanParams {

@@ -181,11 +181,15 @@ def test_every_tile_shape(ctx, shape, kt, vt):
 
 
 @pytest.mark.parametrize("n", [1, 3, 1001, 65537, (1 << 20) + 5])
-def test_pinned_host_buffers(ctx, n):
-    """GS_FLAG_HOST with pinned host memory: the transfers run as copy kernels
-    over the CPU-GPU link (unaligned views fall back to the copy engine)."""
+@pytest.mark.parametrize("dist", ["uniform", "equal"])
+def test_pinned_host_buffers(ctx, n, dist):
+    """GS_FLAG_HOST with pinned host memory. On the radix path the upsweep
+    reads the input across the CPU-GPU link and keeps the device copy the
+    passes sort (all-equal keys: every digit trivial); the SampleSort shape
+    moves the buffers with copy kernels. Outputs go back by copy kernel (an
+    unaligned view falls back to the copy engine)."""
     import torch
-    a = datagen.host("uniform", n, np.uint32, seed=n)
+    a = datagen.host(dist, n, np.uint32, seed=n)
     v = np.arange(n, dtype=np.uint32)
     for off in (0, 1):  # off 1: 4-byte offset, not 16-byte aligned
         hk = torch.empty(n + off, dtype=torch.int32, pin_memory=True)
@@ -194,13 +198,20 @@ def test_pinned_host_buffers(ctx, n):
         vo = torch.empty(n + off, dtype=torch.int32, pin_memory=True)
         hk[off:].copy_(torch.from_numpy(a.view(np.int32)))
         hv[off:].copy_(torch.from_numpy(v.view(np.int32)))
-        st = ctx.sort_keys(hk[off:], ko[off:], dtype=np.uint32, flags=capi.FLAG_HOST)
-        assert st == capi.GS_OK, ctx.last_error()
-        assert same_bits(ko[off:].numpy().view(np.uint32), oracle.sort_keys(a))
-        st = ctx.sort_pairs(hk[off:], hv[off:], ko[off:], vo[off:], key_dtype=np.uint32,
-                            val_dtype=np.uint32, descending=True, stable=True,
-                            flags=capi.FLAG_HOST)
-        assert st == capi.GS_OK, ctx.last_error()
-        wk, wv = oracle.sort_pairs(a, v, True, True)
-        assert same_bits(ko[off:].numpy().view(np.uint32), wk)
-        assert same_bits(vo[off:].numpy().view(np.uint32), wv)
+        for algo in (capi.ALGO_AUTO, capi.ALGO_SAMPLE):
+            ko.zero_()
+            st = ctx.sort_keys(hk[off:], ko[off:], dtype=np.uint32, flags=capi.FLAG_HOST,
+                               algo=algo)
+            assert st == capi.GS_OK, ctx.last_error()
+            assert same_bits(ko[off:].numpy().view(np.uint32), oracle.sort_keys(a))
+        for desc, stable in ((True, True), (False, False)):
+            ko.zero_()
+            vo.zero_()
+            st = ctx.sort_pairs(hk[off:], hv[off:], ko[off:], vo[off:], key_dtype=np.uint32,
+                                val_dtype=np.uint32, descending=desc, stable=stable,
+                                flags=capi.FLAG_HOST)
+            assert st == capi.GS_OK, ctx.last_error()
+            wk, wv = oracle.sort_pairs(a, v, desc, stable)
+            assert same_bits(ko[off:].numpy().view(np.uint32), wk)
+            assert same_bits(vo[off:].numpy().view(np.uint32), wv)
+        assert same_bits(hk[off:].numpy().view(np.uint32), a)  # input untouched
