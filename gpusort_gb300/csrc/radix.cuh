@@ -172,7 +172,15 @@ struct PassConfig {
   static constexpr size_t VAL_BYTES = HAS_V ? sizeof(typename std::conditional<HAS_V, V, uint32_t>::type) : 0;
   static constexpr size_t SMEM_KEYS = size_t(TILE) * sizeof(K);
   static constexpr size_t SMEM_VALS = size_t(TILE) * VAL_BYTES;
-  static constexpr size_t DYN_SMEM = SMEM_KEYS + SMEM_VALS;
+  // Dynamic shared memory: the ranking table (per warp and digit, 64-bit)
+  // and the reorder staging of the tile are never live at the same time,
+  // so they share one region; the per-warp digit offsets, live from the
+  // count phase to the end of the reorder, follow it.
+  static constexpr size_t TAB_BYTES = size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t);
+  static constexpr size_t STAGE_BYTES = SMEM_KEYS + SMEM_VALS;
+  static constexpr size_t UNION_BYTES = ((STAGE_BYTES > TAB_BYTES ? STAGE_BYTES : TAB_BYTES) + 15) & ~size_t(15);
+  static constexpr size_t OFF_BYTES = size_t(WARPS) * RADIX * sizeof(uint32_t);
+  static constexpr size_t DYN_SMEM = UNION_BYTES + OFF_BYTES;
 };
 
 
@@ -213,12 +221,15 @@ pass_kernel(PassParams p) {
   using VS = typename std::conditional<HAS_V, V, uint32_t>::type;  // storage type
 
   extern __shared__ __align__(16) uint8_t s_dyn[];
+  // Ranking table, in the region the reorder stages the tile in later.
   // Stable ranking: per warp and digit, the peer mask of the current item
   // row and the running count (mask in the low half for even digits, in the
-  // high half for odd ones). After ranking, [31:0] becomes the digit's start
-  // in the tile for that warp. The unstable ranking uses the
-  // first RADIX+1 words as tile counters, later tile offsets.
-  __shared__ __align__(16) uint64_t s_tab[WARPS][RADIX + 1];
+  // high half for odd ones). The unstable ranking uses its first RADIX
+  // 32-bit words as tile counters.
+  uint64_t (*const s_tab)[RADIX + 1] = reinterpret_cast<uint64_t (*)[RADIX + 1]>(s_dyn);
+  // Per warp and digit: the warp's start of the digit in the tile (stable
+  // ranking); row 0 holds the tile offsets of the unstable ranking.
+  uint32_t (*const s_offd)[RADIX] = reinterpret_cast<uint32_t (*)[RADIX]>(s_dyn + Cfg::UNION_BYTES);
   __shared__ uint32_t s_dst_base[RADIX];
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
@@ -424,7 +435,7 @@ pass_kernel(PassParams p) {
       for (int w = 0; w < WARPS; ++w) {
         const uint64_t e = s_tab[w][tid];
         const uint32_t c = (tid & 1) ? uint32_t(e) : uint32_t(e >> 32);
-        s_tab[w][tid] = run;  // this thread owns column tid
+        s_offd[w][tid] = run;  // this thread owns column tid
         run += c;
       }
       count = run;
@@ -520,10 +531,10 @@ pass_kernel(PassParams p) {
       atomicOr(p.err, ERR_SCATTER_RANGE);
     }
     if (unstable) {
-      s_cnt[tid] = tile_excl;
+      s_offd[0][tid] = tile_excl;
     } else {
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) s_tab[w][tid] += tile_excl;
+      for (int w = 0; w < WARPS; ++w) s_offd[w][tid] += tile_excl;
     }
   }
   __syncthreads();
@@ -531,12 +542,12 @@ pass_kernel(PassParams p) {
   // Reorder the tile in shared memory by digit (keys in transformed form).
   K* s_keys = reinterpret_cast<K*>(s_dyn);
   VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
-  const uint32_t* s_off = reinterpret_cast<const uint32_t*>(&s_tab[warp][0]);
+  const uint32_t* s_off = s_offd[unstable ? 0 : warp];
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     if (wloc + 32 * i < tile_n) {
       const uint32_t d = digit_at(i);
-      const uint32_t start = unstable ? s_cnt[d] : s_off[2 * d];
+      const uint32_t start = s_off[d];
       const uint32_t pos = start + get_rank(i);
       s_keys[pos] = keys[i];
       if constexpr (HAS_V) s_vals[pos] = vals[i];
