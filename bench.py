@@ -165,6 +165,22 @@ def cpu_baseline(keys_sample: np.ndarray, budget_s: float, threads_total: int | 
             "seconds": t, "sorted": ok}
 
 
+def max_over_ranks(t_ms: float, world: int, device=None) -> float:
+    """The slowest rank's time (replicas are timed together; one rank: t_ms)."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_gkeys(n_per_rank: int, world: int, t_ms: float) -> float:
+    """Keys sorted by all replicas per second (Gkeys/s) over the slowest rank's time."""
+    return world * n_per_rank / (t_ms * 1e-3) / 1e9
+
+
 def time_steps(fn, stream, steps: int, warmup: int) -> float:
     """Average ms of fn() over `steps` runs after `warmup`, CUDA events on
     `stream` (the stream the engine launches on)."""
@@ -397,12 +413,8 @@ def main():
     st = ctx.status_synchronize()
     if st != capi.GS_OK:
         raise RuntimeError(ctx.last_error())
-    t_ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = world * n / (t_ms * 1e-3) / 1e9
+    t_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, device="cuda")
+    value = whole_job_gkeys(n, world, t_ms)
 
     # per-kernel times of the pipeline (events recorded by the engine on the
     # launching stream), a separate short loop
