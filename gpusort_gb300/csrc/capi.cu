@@ -393,6 +393,17 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
                       uint64_t n, uint32_t flags, const HostFuse* fuse = nullptr) {
   const bool desc = flags & GS_FLAG_DESCENDING;
   const bool stable = flags & GS_FLAG_PAIRS_STABLE;
+  // Few keys and no payload: one CTA sorts them in shared memory (one launch
+  // instead of the radix pipeline's five). An explicit pass shape, timing
+  // marks or an injected stall ask for the radix pipeline itself.
+  if (vb == 0 && n <= gs::small_sort_max() && ctx->shape < 0 && !ctx->timing &&
+      !ctx->inject_stall) {
+    // (With pinned host input, kin is its device mapping: the CTA reads it
+    // across the link directly.)
+    cudaError_t e = gs::launch_small_sort(kin, kout, uint32_t(n), kb, kkind, desc, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "small sort launch");
+    return GS_OK;
+  }
   gs::RadixJob job;
   job.keys_in = kin;
   job.keys_out = kout;

@@ -96,6 +96,12 @@ cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void*
                          uint64_t* status, uint32_t* gen_counter, uint32_t* err,
                          uint32_t spin_limit, const DeviceProps& props, cudaStream_t st);
 
+// Sort n <= small_sort_max() keys (no payload) in one CTA's shared memory;
+// `in` may equal `out`.
+uint32_t small_sort_max();
+cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_bytes,
+                              uint32_t kind, bool desc, cudaStream_t st);
+
 // Sample-sort bucketing (keys only): sample + splitters + bucket histogram
 // + one bucket scatter pass from job.keys_in to job.keys_out (which must
 // differ). job.work->hist[0][0..parts) holds the bucket sizes afterwards.

@@ -39,10 +39,11 @@ struct SegGroup {
 struct GroupSortParams {
   const void* in;
   void* out;
-  const SegGroup* groups;
+  const SegGroup* groups;          // null: one group of single_count elements
   const uint32_t* seg_starts_rel;  // per group: nsegs + 1 offsets relative to start
   uint32_t key_kind;
   uint32_t desc;
+  uint32_t single_count;
 };
 
 // One CTA sorts one group in shared memory: LSD passes over the key's
@@ -65,13 +66,14 @@ group_sort_kernel(GroupSortParams p) {
   __shared__ uint32_t s_sstart[GROUP_MAX_SEGS + 1];
   __shared__ uint32_t s_tmp[8];
 
-  const SegGroup g = p.groups[blockIdx.x];
+  const SegGroup g = p.groups ? p.groups[blockIdx.x] : SegGroup{0, p.single_count, 0, 1, 0};
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const K* in = static_cast<const K*>(p.in) + g.start;
   K* out = static_cast<K*>(p.out) + g.start;
   const uint32_t cnt = g.count;
-  for (uint32_t i = tid; i <= g.nsegs; i += THREADS) s_sstart[i] = p.seg_starts_rel[g.first_seg + i];
+  for (uint32_t i = tid; i <= g.nsegs; i += THREADS)
+    s_sstart[i] = p.groups ? p.seg_starts_rel[g.first_seg + i] : (i == 0 ? 0u : cnt);
   __syncthreads();
   // Load (transformed) keys and local segment ids.
   for (uint32_t i = tid; i < cnt; i += THREADS) {
@@ -400,6 +402,30 @@ cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void*
   if (pl->key_bytes == 4)
     return seg_run_t<uint32_t>(pl, in, out, alt, status, gen_counter, err, spin_limit, props, st);
   return seg_run_t<uint64_t>(pl, in, out, alt, status, gen_counter, err, spin_limit, props, st);
+}
+
+uint32_t small_sort_max() { return GROUP_KEYS; }
+
+// One CTA sorts n <= GROUP_KEYS keys in shared memory (the batched sort's
+// group kernel with a single group): one launch instead of the radix
+// pipeline's five. Reads all of `in` before writing `out`, so they may alias.
+cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_bytes,
+                              uint32_t kind, bool desc, cudaStream_t st) {
+  if (n == 0 || n > GROUP_KEYS) return cudaErrorInvalidValue;
+  GroupSortParams gp{in, out, nullptr, nullptr, kind, uint32_t(desc), n};
+  auto go = [&](auto kern, size_t dyn, bool& attr) -> cudaError_t {
+    if (!attr) {
+      const cudaError_t e =
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    kern<<<1, GROUP_THREADS, dyn, st>>>(gp);
+    return cudaGetLastError();
+  };
+  static bool attr32 = false, attr64 = false;
+  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>(), attr32);
+  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>(), attr64);
 }
 
 }  // namespace gs

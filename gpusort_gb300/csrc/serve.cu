@@ -214,7 +214,12 @@ void start(gs_server* s, Slot& sl) {
   job.err = sl.err;
   job.shape = gs::radix_default_shape(r->kb, r->vb);
   uint32_t gen_unused = 0;
-  if (e == cudaSuccess) e = gs::launch_radix_sort(job, s->props, &gen_unused, sl.stream);
+  if (e == cudaSuccess) {
+    if (!r->has_v && n <= gs::small_sort_max())  // one CTA in shared memory
+      e = gs::launch_small_sort(kin, kout, uint32_t(n), r->kb, r->kk, job.desc, sl.stream);
+    else
+      e = gs::launch_radix_sort(job, s->props, &gen_unused, sl.stream);
+  }
   if (r->host) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(r->kout, kout, kbytes, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess && r->has_v)
