@@ -20,7 +20,6 @@ enum KeyKind : uint32_t { KIND_UNSIGNED = 0, KIND_SIGNED = 1, KIND_FLOAT = 2 };
 enum ErrBits : uint32_t {
   ERR_LOOKBACK_TIMEOUT = 1u,
   ERR_SCATTER_RANGE = 2u,
-  ERR_COPY_TIMEOUT = 4u,
   ERR_SMEM_ALIGN = 8u
 };
 
@@ -92,51 +91,9 @@ __device__ __forceinline__ uint64_t ld_stream(const uint64_t* p) {
   return v;
 }
 
-// --- Bulk async copies (TMA, 1-D) tracked by shared-memory mbarriers.
+// Shared-memory address of a generic pointer (alignment checks).
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-               : "memory");
-}
-// Make mbarrier initialisation visible to the async (TMA) proxy.
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// Order this thread's earlier shared-memory accesses before later
-// async-proxy (TMA) writes to the same memory.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-// Global -> shared bulk copy; both addresses 16-byte aligned, bytes % 16 == 0.
-__device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src_gmem, uint32_t bytes,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(dst_smem)),
-      "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-// Wait for phase `parity` of `bar`, at most `limit` polls; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
-  const uint32_t addr = smem_addr(bar);
-  for (uint32_t i = 0; i < limit; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
-        "selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
