@@ -101,6 +101,19 @@ cudaError_t seg_plan_run(const gs_seg_plan* pl, const void* in, void* out, void*
 uint32_t small_sort_max();
 cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_bytes,
                               uint32_t kind, bool desc, cudaStream_t st);
+// One small keys-only array of a batch (n <= small_sort_max()).
+struct SmallSortReq {
+  const void* in;
+  void* out;
+  uint32_t n;
+  uint32_t kind;
+  uint32_t desc;
+  uint32_t pad;
+};
+// Sort `count` such arrays of one key width in one launch; `reqs` must be
+// readable by the device (device memory or mapped pinned host memory).
+cudaError_t launch_small_sort_batch(const SmallSortReq* reqs, uint32_t count, int key_bytes,
+                                    cudaStream_t st);
 
 // Sample-sort bucketing (keys only): sample + splitters + bucket histogram
 // + one bucket scatter pass from job.keys_in to job.keys_out (which must

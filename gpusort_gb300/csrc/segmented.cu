@@ -44,6 +44,7 @@ struct GroupSortParams {
   uint32_t key_kind;
   uint32_t desc;
   uint32_t single_count;
+  const SmallSortReq* reqs;        // set: CTA b sorts the independent array reqs[b]
 };
 
 // One CTA sorts one group in shared memory: LSD passes over the key's
@@ -66,11 +67,13 @@ group_sort_kernel(GroupSortParams p) {
   __shared__ uint32_t s_sstart[GROUP_MAX_SEGS + 1];
   __shared__ uint32_t s_tmp[8];
 
-  const SegGroup g = p.groups ? p.groups[blockIdx.x] : SegGroup{0, p.single_count, 0, 1, 0};
+  const SmallSortReq* rq = p.reqs ? p.reqs + blockIdx.x : nullptr;
+  const SegGroup g = rq ? SegGroup{0, rq->n, 0, 1, 0}
+                   : p.groups ? p.groups[blockIdx.x] : SegGroup{0, p.single_count, 0, 1, 0};
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const OrderXform<K> kx(p.key_kind, p.desc != 0);
-  const K* in = static_cast<const K*>(p.in) + g.start;
-  K* out = static_cast<K*>(p.out) + g.start;
+  const OrderXform<K> kx(rq ? rq->kind : p.key_kind, (rq ? rq->desc : p.desc) != 0);
+  const K* in = static_cast<const K*>(rq ? rq->in : p.in) + g.start;
+  K* out = static_cast<K*>(rq ? rq->out : p.out) + g.start;
   const uint32_t cnt = g.count;
   for (uint32_t i = tid; i <= g.nsegs; i += THREADS)
     s_sstart[i] = p.groups ? p.seg_starts_rel[g.first_seg + i] : (i == 0 ? 0u : cnt);
@@ -412,7 +415,7 @@ uint32_t small_sort_max() { return GROUP_KEYS; }
 cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_bytes,
                               uint32_t kind, bool desc, cudaStream_t st) {
   if (n == 0 || n > GROUP_KEYS) return cudaErrorInvalidValue;
-  GroupSortParams gp{in, out, nullptr, nullptr, kind, uint32_t(desc), n};
+  GroupSortParams gp{in, out, nullptr, nullptr, kind, uint32_t(desc), n, nullptr};
   auto go = [&](auto kern, size_t dyn, bool& attr) -> cudaError_t {
     if (!attr) {
       const cudaError_t e =
@@ -421,6 +424,27 @@ cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_byt
       attr = true;
     }
     kern<<<1, GROUP_THREADS, dyn, st>>>(gp);
+    return cudaGetLastError();
+  };
+  static bool attr32 = false, attr64 = false;
+  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>(), attr32);
+  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>(), attr64);
+}
+
+// One launch sorting `count` independent small arrays, one CTA each (their
+// descriptors in memory the device can read: device or mapped host memory).
+cudaError_t launch_small_sort_batch(const SmallSortReq* reqs, uint32_t count, int key_bytes,
+                                    cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  GroupSortParams gp{nullptr, nullptr, nullptr, nullptr, 0, 0, 0, reqs};
+  auto go = [&](auto kern, size_t dyn, bool& attr) -> cudaError_t {
+    if (!attr) {
+      const cudaError_t e =
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    kern<<<count, GROUP_THREADS, dyn, st>>>(gp);
     return cudaGetLastError();
   };
   static bool attr32 = false, attr64 = false;

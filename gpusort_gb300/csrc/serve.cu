@@ -19,6 +19,11 @@
 //   A request that does not fit yet holds the head of the queue, so large
 //   requests are not starved by smaller ones behind them. Kernel launches
 //   happen outside the lock, so submitters never wait on the GPU.
+// * Batching: small requests (device memory, keys only, at most 4096 keys)
+//   need no scratch. The ones queued together behind each other, of one key
+//   width, take one slot and run as one launch: one CTA per request sorts it
+//   in shared memory, reading its descriptor from the slot's mapped pinned
+//   array.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -97,6 +102,7 @@ struct Request {
   int kb = 4, vb = 0;
   uint32_t kk = 0, vk = 0;
   uint64_t off = 0, bytes = 0;  // arena range
+  bool small = false;           // device keys-only of <= small_sort_max keys: batched
   Clock::time_point t_submit, t_done;
   State state = State::QUEUED;
   gs_status status = GS_OK;
@@ -109,10 +115,16 @@ struct Slot {
   uint64_t* status = nullptr;
   uint32_t* err = nullptr;
   uint32_t* h_err = nullptr;  // pinned
-  Request* req = nullptr;
+  gs::SmallSortReq* h_reqs = nullptr;        // pinned, device-mapped batch descriptors
+  gs::SmallSortReq* d_reqs = nullptr;        // the device's view of h_reqs
+  std::vector<Request*> batch;               // running requests; empty: idle
   bool finished = false;
   bool launch_failed = false;
 };
+
+// Small requests (device memory, keys only, at most small_sort_max keys) of
+// one key width that are queued together run in one launch, one CTA each.
+constexpr uint32_t MAX_BATCH = 256;
 
 bool dtype_info(gs_dtype t, int* bytes, uint32_t* kind) {
   switch (t) {
@@ -162,13 +174,42 @@ void CUDART_CB slot_done(void* p) {
   gs_server* s = sl->server;
   std::lock_guard<std::mutex> lock(s->mu);
   sl->finished = true;
-  if (sl->req) sl->req->t_done = Clock::now();
+  const auto now = Clock::now();
+  for (Request* r : sl->batch) r->t_done = now;
   notify_locked(s);
+}
+
+// Enqueue a batch of small requests: one launch sorts each in its own CTA.
+void start_small(gs_server* s, Slot& sl) {
+  const uint32_t count = uint32_t(sl.batch.size());
+  for (uint32_t i = 0; i < count; ++i) {
+    const Request* r = sl.batch[i];
+    sl.h_reqs[i] = gs::SmallSortReq{r->kin, r->kout, uint32_t(r->n), r->kk,
+                                    (r->flags & GS_FLAG_DESCENDING) ? 1u : 0u, 0u};
+  }
+  cudaError_t e = cudaMemsetAsync(sl.err, 0, sizeof(uint32_t), sl.stream);
+  if (e == cudaSuccess) e = gs::launch_small_sort_batch(sl.d_reqs, count, sl.batch[0]->kb, sl.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sl.h_err, sl.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, sl.stream);
+  if (e == cudaSuccess) e = cudaLaunchHostFunc(sl.stream, slot_done, &sl);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamSynchronize(sl.stream);
+    std::lock_guard<std::mutex> lock(s->mu);
+    sl.launch_failed = true;
+    sl.finished = true;
+    for (Request* r : sl.batch) r->t_done = Clock::now();
+    notify_locked(s);
+  }
 }
 
 // Enqueue a request's work on its slot (owner thread, lock not held).
 void start(gs_server* s, Slot& sl) {
-  Request* r = sl.req;
+  if (sl.batch[0]->small) {
+    start_small(s, sl);
+    return;
+  }
+  Request* r = sl.batch[0];
   uint8_t* base = s->arena.base + r->off;
   const uint64_t n = r->n, kbytes = n * r->kb, vbytes = n * r->vb;
   const void* kin = r->kin;
@@ -241,15 +282,17 @@ void start(gs_server* s, Slot& sl) {
 
 // Retire a finished slot (lock held).
 void finish_locked(gs_server* s, Slot& sl) {
-  Request* r = sl.req;
-  if (sl.launch_failed) r->status = GS_ERR_CUDA;
-  else r->status = *sl.h_err ? GS_ERR_TIMEOUT : GS_OK;
-  s->arena.release(r->off, r->bytes);
-  r->state = State::DONE;
-  s->latencies_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
-  ++s->completed;
-  s->keys_done += r->n;
-  sl.req = nullptr;
+  for (Request* r : sl.batch) {
+    if (sl.launch_failed) r->status = GS_ERR_CUDA;
+    else r->status = *sl.h_err ? GS_ERR_TIMEOUT : GS_OK;
+    if (r->bytes) s->arena.release(r->off, r->bytes);
+    r->state = State::DONE;
+    s->latencies_ms.push_back(
+        std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+    ++s->completed;
+    s->keys_done += r->n;
+  }
+  sl.batch.clear();
   sl.finished = false;
   sl.launch_failed = false;
   s->done_cv.notify_all();
@@ -263,20 +306,31 @@ void run_loop(gs_server* s) {
     const uint64_t seen = s->events;
     bool busy = false;
     for (Slot& sl : s->slots) {
-      if (sl.req && sl.finished) finish_locked(s, sl);
-      busy |= sl.req != nullptr;
+      if (!sl.batch.empty() && sl.finished) finish_locked(s, sl);
+      busy |= !sl.batch.empty();
     }
     to_start.clear();
     for (Slot& sl : s->slots) {
       if (s->queue.empty()) break;
-      if (sl.req) continue;
+      if (!sl.batch.empty()) continue;
       Request* r = s->queue.front();
-      uint64_t off = 0;
-      if (!s->arena.alloc(r->bytes, &off)) break;  // holds the head
-      r->off = off;
-      r->state = State::RUNNING;
-      s->queue.pop_front();
-      sl.req = r;
+      if (r->small) {  // this and the small requests right behind it, one launch
+        const int kb = r->kb;
+        while (!s->queue.empty() && s->queue.front()->small && s->queue.front()->kb == kb &&
+               sl.batch.size() < MAX_BATCH) {
+          Request* q = s->queue.front();
+          q->state = State::RUNNING;
+          s->queue.pop_front();
+          sl.batch.push_back(q);
+        }
+      } else {
+        uint64_t off = 0;
+        if (!s->arena.alloc(r->bytes, &off)) break;  // holds the head
+        r->off = off;
+        r->state = State::RUNNING;
+        s->queue.pop_front();
+        sl.batch.push_back(r);
+      }
       to_start.push_back(&sl);
     }
     if (!to_start.empty()) {
@@ -298,6 +352,7 @@ void free_server(gs_server* s) {
     if (sl.status) cudaFree(sl.status);
     if (sl.err) cudaFree(sl.err);
     if (sl.h_err) cudaFreeHost(sl.h_err);
+    if (sl.h_reqs) cudaFreeHost(sl.h_reqs);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   if (s->arena.base) cudaFree(s->arena.base);
@@ -349,6 +404,10 @@ gs_server* gs_server_create(int device, const gs_server_opts* opts) {
          cudaMalloc(&sl.status, status_bytes) == cudaSuccess &&
          cudaMalloc(&sl.err, ALIGN) == cudaSuccess &&
          cudaMallocHost(&sl.h_err, sizeof(uint32_t)) == cudaSuccess &&
+         cudaHostAlloc(&sl.h_reqs, MAX_BATCH * sizeof(gs::SmallSortReq), cudaHostAllocMapped) ==
+             cudaSuccess &&
+         cudaHostGetDevicePointer(reinterpret_cast<void**>(&sl.d_reqs), sl.h_reqs, 0) ==
+             cudaSuccess &&
          cudaMemset(sl.work, 0, gs::sort_work_bytes()) == cudaSuccess &&
          cudaMemset(sl.status, 0, status_bytes) == cudaSuccess;
   }
@@ -417,7 +476,8 @@ gs_status gs_server_submit(gs_server* s, gs_dtype key_dtype, int has_values, gs_
     }
   }
   const uint64_t kbytes = align_up(n * r.kb), vbytes = align_up(n * r.vb);
-  r.bytes = (r.host ? 2 : 1) * (kbytes + vbytes);
+  r.small = !r.host && !r.has_v && n <= gs::small_sort_max();
+  r.bytes = r.small ? 0 : (r.host ? 2 : 1) * (kbytes + vbytes);
   if (r.bytes > s->arena.size) return fail(GS_ERR_OOM, "request larger than the HBM budget");
   r.kin = keys_in;
   r.vin = r.has_v ? vals_in : nullptr;
@@ -485,7 +545,7 @@ gs_status gs_server_get_stats(gs_server* s, gs_server_stats* out, int reset) {
   st.completed = s->completed;
   st.keys_done = s->keys_done;
   st.queued = s->queue.size();
-  for (const Slot& sl : s->slots) st.running += sl.req != nullptr;
+  for (const Slot& sl : s->slots) st.running += sl.batch.size();
   st.arena_used = s->arena.used;
   st.arena_peak = s->arena.peak;
   st.p50_ms = pct(0.50);

@@ -314,6 +314,8 @@ uint64_t gs_partition_block(uint64_t n, int nparts);
  *   slots and arena space free up (a request that does not fit yet holds
  *   the head of the queue), so work of requests that arrive while others
  *   run overlaps on the device.
+ * - small requests (device memory, keys only, at most 4096 keys) that are
+ *   queued together run in one launch, one CTA each.
  * Requests are sorts of keys or (key, value) pairs with the flags of
  * gs_sort_pairs (GS_FLAG_DESCENDING, GS_FLAG_PAIRS_STABLE). By default the
  * pointers are device memory on the server's device, which stays the

@@ -178,3 +178,28 @@ def test_poisson_load_small(ctx):
         want = oracle.sort_keys(_bits(r.keys, r.spec.key_dtype)) if r.vals is None else \
             oracle.sort_pairs(_bits(r.keys, r.spec.key_dtype), _bits(r.vals, np.uint32))[0]
         assert same_bits(_bits(r.keys_out, r.spec.key_dtype), want)
+
+
+def test_small_requests_batched_in_one_launch(ctx):
+    """Small device requests (keys only, <= 4096 keys) queued together run
+    as one launch, one CTA each; interleaved key widths split the batches.
+    Every output equals the oracle's."""
+    rng = np.random.default_rng(17)
+    kinds = [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64]
+    jobs = []
+    with capi.Server(0, hbm_budget=256 << 20, max_request_keys=1 << 20, slots=2) as srv:
+        for i in range(300):
+            dt = kinds[int(rng.integers(len(kinds)))]
+            n = int(rng.integers(1, 4097)) if i % 25 else 300000  # a few large ones
+            a = datagen.host("uniform" if i % 3 else "distinct8", n, dt, seed=500 + i)
+            desc = bool(i % 2)
+            d_in = to_dev(a)
+            d_out = d_in if i % 7 == 0 else empty_dev(n, dt)  # some in place
+            rid = srv.submit(d_in, d_out, key_dtype=dt, descending=desc)
+            jobs.append((rid, a, d_out, dt, desc))
+        for rid, a, d_out, dt, desc in jobs:
+            assert srv.poll(rid, wait=True)[0] == capi.GS_OK
+        st = srv.stats()
+        assert st["completed"] == len(jobs) and st["running"] == 0
+    for rid, a, d_out, dt, desc in jobs:
+        assert same_bits(from_dev(d_out, dt), oracle.sort_keys(a, desc)), (a.size, dt, desc)
