@@ -134,6 +134,10 @@ cudaError_t launch_bucket_pass(const RadixJob& job, const void* splitters, uint3
 cudaError_t launch_merge_pass(const void* in, void* out, uint64_t n, uint64_t run, int key_bytes,
                               uint32_t key_kind, bool desc, cudaStream_t st);
 
+// Allow `kern` up to `bytes` of dynamic shared memory on the current device
+// (once per kernel and device; safe to call from any thread).
+cudaError_t allow_dynamic_smem(const void* kern, size_t bytes);
+
 // Set the message gs_last_global_error() returns on this thread.
 void set_last_global_error(const std::string& msg);
 

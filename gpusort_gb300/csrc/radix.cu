@@ -1,4 +1,8 @@
 // Launchers of the onesweep radix pipeline (kernels in radix.cuh).
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "engine.h"
 #include "radix.cuh"
 
@@ -98,13 +102,8 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   using Cfg = PassConfig<K, V, PASS_THREADS, ITEMS>;
   cudaError_t e = cudaSuccess;
   auto kern = pass_kernel<K, V, PASS_THREADS, ITEMS, MINB, CLUSTER>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(Cfg::DYN_SMEM));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
+  if (e != cudaSuccess) return e;
   if (sj != nullptr && CLUSTER > 1) return cudaErrorInvalidValue;
   const uint64_t tiles = sj != nullptr ? sj->total_tiles : (job.n + Cfg::TILE - 1) / Cfg::TILE;
   const uint64_t units = (tiles + CLUSTER - 1) / CLUSTER;  // look-back units (cluster-tiles)
@@ -191,12 +190,8 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   auto ukern = cl == 4 ? upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 4>
              : cl == 3 ? upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 3>
                        : upsweep_kernel<K, V, UPSWEEP_THREADS, UPSWEEP_UNROLL, 2>;
-  static bool uattr[5] = {false, false, false, false, false};
-  if (!uattr[cl]) {
-    e = cudaFuncSetAttribute(ukern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(UPSWEEP_SMEM));
-    if (e != cudaSuccess) return e;
-    uattr[cl] = true;
-  }
+  e = allow_dynamic_smem(reinterpret_cast<const void*>(ukern), UPSWEEP_SMEM);
+  if (e != cudaSuccess) return e;
   const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
   uint64_t ublocks = (job.n + chunk - 1) / chunk;
   const uint64_t umax = uint64_t(props.num_sms) * UPSWEEP_PER_SM;
@@ -277,13 +272,8 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.in_place = 0;
   plan_kernel<<<1, 256, 0, st>>>(pp);
   auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, 1, true>;
-  static bool attr = false;
-  cudaError_t e = cudaSuccess;
-  if (!attr) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::DYN_SMEM));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
+  if (e != cudaSuccess) return e;
   PassParams pa{};
   pa.keys_in = job.keys_in;
   pa.keys_out = job.keys_out;
@@ -318,6 +308,19 @@ uint32_t radix_tile(int key_bytes, int val_bytes) {
 }
 
 int radix_num_shapes() { return NUM_SHAPES; }
+
+cudaError_t allow_dynamic_smem(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({kern, dev})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess) done.insert({kern, dev});
+  return e;
+}
 
 namespace {
 template <typename K, typename V>

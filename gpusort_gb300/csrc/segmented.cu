@@ -356,13 +356,8 @@ cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* al
   if (pl->ngroups) {
     GroupSortParams gp{in, out, pl->d_groups, pl->d_starts_rel, pl->kind, pl->desc};
     constexpr size_t dyn = group_sort_dyn_smem<K>();
-    static bool attr = false;
-    if (!attr) {
-      e = cudaFuncSetAttribute(group_sort_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(dyn));
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+    e = allow_dynamic_smem(reinterpret_cast<const void*>(group_sort_kernel<K>), dyn);
+    if (e != cudaSuccess) return e;
     group_sort_kernel<K><<<pl->ngroups, GROUP_THREADS, dyn, st>>>(gp);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -416,19 +411,14 @@ cudaError_t launch_small_sort(const void* in, void* out, uint32_t n, int key_byt
                               uint32_t kind, bool desc, cudaStream_t st) {
   if (n == 0 || n > GROUP_KEYS) return cudaErrorInvalidValue;
   GroupSortParams gp{in, out, nullptr, nullptr, kind, uint32_t(desc), n, nullptr};
-  auto go = [&](auto kern, size_t dyn, bool& attr) -> cudaError_t {
-    if (!attr) {
-      const cudaError_t e =
-          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn));
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+  auto go = [&](auto kern, size_t dyn) -> cudaError_t {
+    const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), dyn);
+    if (e != cudaSuccess) return e;
     kern<<<1, GROUP_THREADS, dyn, st>>>(gp);
     return cudaGetLastError();
   };
-  static bool attr32 = false, attr64 = false;
-  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>(), attr32);
-  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>(), attr64);
+  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>());
+  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>());
 }
 
 // One launch sorting `count` independent small arrays, one CTA each (their
@@ -437,19 +427,14 @@ cudaError_t launch_small_sort_batch(const SmallSortReq* reqs, uint32_t count, in
                                     cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   GroupSortParams gp{nullptr, nullptr, nullptr, nullptr, 0, 0, 0, reqs};
-  auto go = [&](auto kern, size_t dyn, bool& attr) -> cudaError_t {
-    if (!attr) {
-      const cudaError_t e =
-          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn));
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
+  auto go = [&](auto kern, size_t dyn) -> cudaError_t {
+    const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), dyn);
+    if (e != cudaSuccess) return e;
     kern<<<count, GROUP_THREADS, dyn, st>>>(gp);
     return cudaGetLastError();
   };
-  static bool attr32 = false, attr64 = false;
-  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>(), attr32);
-  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>(), attr64);
+  if (key_bytes == 4) return go(group_sort_kernel<uint32_t>, group_sort_dyn_smem<uint32_t>());
+  return go(group_sort_kernel<uint64_t>, group_sort_dyn_smem<uint64_t>());
 }
 
 }  // namespace gs
