@@ -1,0 +1,86 @@
+"""Single runs of each sort path on synthetic uniform keys, for profiling the
+kernels one path launches:
+
+    python -m gpusort_gb300.workloads {radix,hyk,sample,segmented,gather,host}
+        [--log2n N] [--runs R]
+
+* radix      - gs_sort_keys, onesweep radix (upsweep, plan, passes)
+* hyk        - GS_ALGO_HYK, p=4, k=4 (partition sorts, merge-path merges)
+* sample     - GS_ALGO_SAMPLE, p=64, oversample 32 (sample, bucket
+               histogram, bucket scatter pass, per-bucket batched sort)
+* segmented  - a planned batched sort of segments with log-uniform lengths
+               (group sort, per-segment histograms, segmented passes)
+* gather     - gs_gather of 8-byte elements by a random permutation
+* host       - gs_sort_keys with pinned host buffers (GS_FLAG_HOST: upsweep
+               reading across the CPU-GPU link, output by copy kernel)
+
+Each run is synchronous and checked for GS_OK; `--runs` (default 2) lets a
+profiler skip the first run's launches.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+from . import capi, datagen
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("path", choices=["radix", "hyk", "sample", "segmented", "gather", "host"])
+    ap.add_argument("--log2n", type=int, default=26)
+    ap.add_argument("--runs", type=int, default=2)
+    args = ap.parse_args(argv)
+    import torch
+    ctx = capi.Context(0)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    n = 1 << args.log2n
+    a = datagen.device("uniform", n, np.uint32, seed=1)
+    o = torch.empty_like(a)
+
+    def ok(st):
+        if st != capi.GS_OK:
+            raise capi.GsError(st, ctx.last_error())
+
+    sync = capi.FLAG_SYNC
+    for _ in range(args.runs):
+        if args.path == "radix":
+            ok(ctx.sort_keys(a, o, dtype=np.uint32, flags=sync))
+        elif args.path == "hyk":
+            ok(ctx.sort_keys(a, o, dtype=np.uint32, algo=capi.ALGO_HYK, partitions=4, k_way=4,
+                             flags=sync))
+        elif args.path == "sample":
+            ok(ctx.sort_keys(a, o, dtype=np.uint32, algo=capi.ALGO_SAMPLE, partitions=64,
+                             oversample=32, flags=sync))
+    if args.path == "segmented":
+        off = datagen.segment_offsets(max(1, n // 11000), 16, 1 << 22, total=n, seed=8)
+        m = int(off[-1])
+        s = datagen.device("uniform", m, np.uint32, seed=8)
+        so = torch.empty_like(s)
+        plan = ctx.segmented_plan(np.uint32, m, off)
+        try:
+            for _ in range(args.runs):
+                ok(ctx.segmented_run(plan, s, so))
+            ok(ctx.status_synchronize())
+        finally:
+            ctx.segmented_destroy(plan)
+    elif args.path == "gather":
+        perm = torch.randperm(n, device="cuda", dtype=torch.int64)
+        src = torch.empty(n, dtype=torch.int64, device="cuda").random_()
+        dst = torch.empty_like(src)
+        torch.cuda.synchronize()
+        for _ in range(args.runs):
+            ok(ctx.gather(src, dst, perm, 8, flags=sync))
+    elif args.path == "host":
+        h = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        h.copy_(a.cpu())
+        ho = torch.empty(n, dtype=torch.int32, pin_memory=True)  # empty_like would not pin
+        for _ in range(args.runs):
+            ok(ctx.sort_keys(h, ho, dtype=np.uint32, flags=capi.FLAG_HOST))
+    torch.cuda.synchronize()
+    print(args.path, "ok", flush=True)
+
+
+if __name__ == "__main__":
+    main()
