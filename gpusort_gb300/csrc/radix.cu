@@ -261,8 +261,8 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
 template <typename K>
 cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t nsplit,
                           const DeviceProps& props, cudaStream_t st) {
-  using Sh = PassShape<K, NoValue, 0>;
-  static_assert(Sh::CLUSTER == 1, "bucket passes run without clusters");
+  // 16 items per thread leave registers for the packed bucket ids.
+  using Sh = Shape<512, 16, 2, 1>;
   using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS>;
   PlanParams pp{};
   pp.work = job.work;
@@ -272,7 +272,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.in_place = 0;
   plan_kernel<<<1, 256, 0, st>>>(pp);
   auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, 1, true>;
-  cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
+  cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM_BUCKET);
   if (e != cudaSuccess) return e;
   PassParams pa{};
   pa.keys_in = job.keys_in;
@@ -291,7 +291,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pa.splitters = splitters;
   pa.nsplit = nsplit;
   const uint64_t tiles = (job.n + Cfg::TILE - 1) / Cfg::TILE;
-  kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM, st>>>(pa);
+  kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM_BUCKET, st>>>(pa);
   return cudaGetLastError();
 }
 

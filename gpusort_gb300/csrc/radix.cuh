@@ -181,7 +181,22 @@ struct PassConfig {
   static constexpr size_t UNION_BYTES = ((STAGE_BYTES > TAB_BYTES ? STAGE_BYTES : TAB_BYTES) + 15) & ~size_t(15);
   static constexpr size_t OFF_BYTES = size_t(WARPS) * RADIX * sizeof(uint16_t);
   static constexpr size_t DYN_SMEM = UNION_BYTES + OFF_BYTES;
+  // BUCKET mode also stages each element's bucket (one byte) for the scatter.
+  static constexpr size_t DYN_SMEM_BUCKET = DYN_SMEM + size_t(TILE);
 };
+
+// Number of sorted splitters s[0..nsplit) that are <= y (upper_bound), by
+// fixed power-of-two steps: every lane runs the same predicated steps, no
+// divergent branches. nsplit < 256.
+template <typename K>
+__device__ __forceinline__ uint32_t bucket_of(const K* s, uint32_t nsplit, K y) {
+  uint32_t lo = 0;
+  for (uint32_t step = nsplit ? (1u << (31 - __clz(nsplit))) : 0u; step; step >>= 1) {
+    const uint32_t probe = lo + step;
+    if (probe <= nsplit && s[probe - 1] <= y) lo = probe;
+  }
+  return lo;
+}
 
 
 // Keys live in the transformed domain between passes: the first pass that
@@ -336,12 +351,7 @@ pass_kernel(PassParams p) {
   // Digit of order bits: a radix digit, or the bucket (upper_bound).
   auto key_digit = [&](K y) -> uint32_t {
     if constexpr (!BUCKET) return uint32_t(y >> shift) & (RADIX - 1);
-    uint32_t lo = 0, len = nsplit;
-    while (len > 0) {
-      const uint32_t half = len >> 1;
-      if (s_split[lo + half] <= y) { lo += half + 1; len -= half + 1; } else { len = half; }
-    }
-    return lo;
+    return bucket_of(s_split, nsplit, y);
   };
 
   // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
@@ -373,7 +383,17 @@ pass_kernel(PassParams p) {
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) keys[i] = kx.fwd(keys[i]);
   }
+  // BUCKET mode: each item's bucket is searched once and kept, one byte each.
+  uint32_t bdig[BUCKET ? (ITEMS + 3) / 4 : 1];
+  if constexpr (BUCKET) {
+#pragma unroll
+    for (int i = 0; i < (ITEMS + 3) / 4; ++i) bdig[i] = 0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+      if (wloc + 32 * i < tile_n) bdig[i >> 2] |= key_digit(keys[i]) << (8 * (i & 3));
+  }
   auto digit_at = [&](int i) -> uint32_t {
+    if constexpr (BUCKET) return (bdig[i >> 2] >> (8 * (i & 3))) & 0xFFu;
     if constexpr (HAS_V) {
       if (from_val) return uint32_t(vx.fwd(vals[i]) >> shift) & (RADIX - 1);
     }
@@ -544,6 +564,7 @@ pass_kernel(PassParams p) {
   // Reorder the tile in shared memory by digit (keys in transformed form).
   K* s_keys = reinterpret_cast<K*>(s_dyn);
   VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
+  uint8_t* s_bdig = s_dyn + Cfg::DYN_SMEM;  // BUCKET mode only
   const uint16_t* s_off = s_offd[unstable ? 0 : warp];
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
@@ -553,6 +574,7 @@ pass_kernel(PassParams p) {
       const uint32_t pos = start + get_rank(i);
       s_keys[pos] = keys[i];
       if constexpr (HAS_V) s_vals[pos] = vals[i];
+      if constexpr (BUCKET) s_bdig[pos] = uint8_t(d);
     }
   }
   __syncthreads();
@@ -570,6 +592,8 @@ pass_kernel(PassParams p) {
       if constexpr (HAS_V) {
         v = s_vals[r];
         d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1)) : key_digit(k);
+      } else if constexpr (BUCKET) {
+        d = s_bdig[r];
       } else {
         d = key_digit(k);
       }

@@ -95,12 +95,7 @@ __global__ void __launch_bounds__(512) bucket_hist_kernel(BucketHistParams p) {
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
     const K y = kx.fwd(keys[i]);
-    uint32_t lo = 0, len = p.nsplit;
-    while (len > 0) {
-      const uint32_t half = len >> 1;
-      if (s_split[lo + half] <= y) { lo += half + 1; len -= half + 1; } else { len = half; }
-    }
-    atomicAdd(&s_h[lo], 1u);
+    atomicAdd(&s_h[bucket_of(s_split, p.nsplit, y)], 1u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < RADIX; i += blockDim.x)
