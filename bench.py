@@ -438,7 +438,7 @@ def main():
     e2e = None
     if not args.no_e2e:
         h_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        h_in.copy_(keys.cpu() if False else keys.to("cpu", non_blocking=False))
+        h_in.copy_(keys.cpu())
         h_out = torch.empty(n, dtype=torch.int32, pin_memory=True)
         es = []
         for i in range(2 + args.steps):
@@ -450,7 +450,7 @@ def main():
             if i >= 2:
                 es.append(dt)
         e_t = statistics.median(es)
-        e2e_ok = bool(torch.equal(h_out[: 1 << 16].cuda(), out[: 1 << 16]))
+        e2e_ok = bool(torch.equal(h_out.cuda(), out))
         e2e = {"value": n / e_t / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": 4 * n,
                "d2h_bytes_per_step": 4 * n, "ms_per_step": e_t * 1e3,
                "api": "gs_sort_keys(GS_FLAG_HOST), pinned host buffers", "matches_device": e2e_ok}

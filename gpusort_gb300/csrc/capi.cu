@@ -57,6 +57,12 @@ struct gs_ctx {
   cudaEvent_t kev[3 + 16] = {};
   int n_kev = 0;
   uint32_t kev_exec_mask = 0;
+  // Host-buffer sorts in bucket groups (made on first use): the stream the
+  // sorted groups leave on, its events, and the histograms read back.
+  int host_groups = -1;  // -1: by size (host_groups_for); 0 or 1: one sort, then one copy out
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_hist = nullptr, ev_group = nullptr, ev_copied = nullptr;
+  uint32_t* h_hist = nullptr;  // pinned, gs::HIST_WORDS words
 };
 
 namespace gs {
@@ -286,11 +292,15 @@ int parse_tuning(const char* json, std::vector<gs_tuning_entry>* out) {
   return int(out->size());
 }
 
-void phase_reset(gs_ctx* ctx) { ctx->n_phases = 0; }
+// Phase timing of one call: the start is marked before any work is
+// enqueued, and each phase_mark ends the phase named.
+void phase_reset(gs_ctx* ctx) {
+  ctx->n_phases = 0;
+  if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
+}
 
 void phase_mark(gs_ctx* ctx, const char* name) {
   if (!ctx->timing || ctx->n_phases >= 7) return;
-  if (ctx->n_phases == 0) cudaEventRecord(ctx->ev[0], ctx->stream);
   ctx->phase_names[ctx->n_phases] = name;
   ctx->n_phases++;
   cudaEventRecord(ctx->ev[ctx->n_phases], ctx->stream);
@@ -387,6 +397,30 @@ struct HostFuse {
   void* vals_copy = nullptr;
 };
 
+// The parts of a radix job that follow from the element types, the flags
+// and the context (buffers left to the caller).
+gs::RadixJob radix_job(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind, uint64_t n,
+                       uint32_t flags) {
+  const bool desc = flags & GS_FLAG_DESCENDING;
+  const bool stable = flags & GS_FLAG_PAIRS_STABLE;
+  gs::RadixJob job;
+  job.n = n;
+  job.key_bytes = kb;
+  job.val_bytes = vb;
+  job.key_kind = kkind;
+  job.val_kind = vkind;
+  job.desc = desc;
+  job.ties_by_value = vb > 0 && !stable;
+  job.reverse_first = vb > 0 && stable && desc;
+  job.first_unstable = !(vb > 0 && stable);
+  job.work = ctx->work;
+  job.err = ctx->err;
+  job.spin_limit = ctx->spin_limit;
+  job.inject_stall = ctx->inject_stall;
+  job.shape = pass_shape_for(ctx, kb, kkind, vb, n);
+  return job;
+}
+
 // Device-memory radix sort of keys or pairs.
 gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind,
                       const void* kin, const void* vin, void* kout, void* vout,
@@ -404,25 +438,11 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
     if (e != cudaSuccess) return cuda_fail(ctx, e, "small sort launch");
     return GS_OK;
   }
-  gs::RadixJob job;
+  gs::RadixJob job = radix_job(ctx, kb, kkind, vb, vkind, n, flags);
   job.keys_in = kin;
   job.keys_out = kout;
   job.vals_in = vin;
   job.vals_out = vout;
-  job.n = n;
-  job.key_bytes = kb;
-  job.val_bytes = vb;
-  job.key_kind = kkind;
-  job.val_kind = vkind;
-  job.desc = desc;
-  job.ties_by_value = vb > 0 && !stable;
-  job.reverse_first = vb > 0 && stable && desc;
-  job.first_unstable = !(vb > 0 && stable);
-  job.work = ctx->work;
-  job.err = ctx->err;
-  job.spin_limit = ctx->spin_limit;
-  job.inject_stall = ctx->inject_stall;
-  job.shape = pass_shape_for(ctx, kb, kkind, vb, n);
   if (fuse) {
     job.keys_copy = fuse->keys_copy;
     job.vals_copy = fuse->vals_copy;
@@ -563,6 +583,195 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
   return GS_OK;
 }
 
+// Bucket groups of a host sort of n elements (below 2: not grouped).
+// Measured on GB300, 2^30 u32 keys with pinned buffers: 58.7 ms ungrouped,
+// 50.1 / 48.0 / 47.0 / 48.0 ms with 4 / 8 / 16 / 32 groups; 2^26 keys: 3.76
+// ms ungrouped, 3.26 with 4 or 8 groups; at 2^24 and below the grouped
+// path is slower (per-group launches and host round trip).
+uint32_t host_groups_for(const gs_ctx* ctx, uint64_t n) {
+  if (ctx->host_groups >= 0) return n >= 4096 ? uint32_t(ctx->host_groups) : 0u;
+  if (n >= (uint64_t(1) << 28)) return 16;
+  if (n >= (uint64_t(1) << 26)) return 8;
+  if (n >= (uint64_t(1) << 25)) return 4;
+  return 0;
+}
+
+// A run of whole buckets: elements [begin, end), and whether more than one
+// bucket holds elements.
+struct BucketRun {
+  uint64_t begin, end;
+  bool mixed;
+};
+
+// Runs of whole buckets of `counts` (one digit's histogram, in output
+// order) holding about n / groups elements each.
+std::vector<BucketRun> bucket_groups(const uint32_t* counts, uint64_t n, uint32_t groups) {
+  std::vector<BucketRun> out;
+  uint64_t begin = 0, acc = 0;
+  uint32_t filled = 0;
+  for (uint32_t b = 0; b < gs::RADIX; ++b) {
+    acc += counts[b];
+    filled += counts[b] != 0;
+    const bool close = b + 1 == uint32_t(gs::RADIX) ||
+                       acc * groups >= (uint64_t(out.size()) + 1) * n;
+    if (close && acc > begin) {
+      out.push_back({begin, acc, filled > 1});
+      begin = acc;
+      filled = 0;
+    }
+  }
+  return out;
+}
+
+// Sort of pinned host buffers in bucket groups, so that the sort overlaps
+// the transfer out. The upsweep reads the input across the CPU-GPU link
+// into the stage buffer and counts every digit; one pass on the most
+// significant digit t that varies splits the elements into its 256 buckets
+// (stage -> scratch); then runs of buckets are sorted one after another,
+// and every sorted run is copied to the host on a second stream while the
+// next run sorts. A run of one bucket is sorted on the digits below t; a
+// run of several buckets on the digits up to t, since LSD passes on the
+// lower digits alone would undo the split's order (the last pass, on t,
+// restores it with the lower digits as the tie order). The order is the one
+// device_sort gives: the split pass is stable exactly when the first pass
+// of device_sort would be (and reads back to front when that one does),
+// and each run is a whole sort on every digit that varies within it.
+gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, const void* mk,
+                           const void* mv, void* kout, void* vout, uint64_t n, uint32_t flags,
+                           uint32_t groups) {
+  if (!ctx->copy_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_hist, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_group, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+      e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_hist), sizeof(uint32_t) * gs::HIST_WORDS,
+                        cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "host-sort stream setup");
+  }
+  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st == GS_OK && vb) st = ensure(ctx, ctx->alt_v, size_t(n) * vb);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), 0);
+  if (st != GS_OK) return st;
+  uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
+  uint8_t* sv = static_cast<uint8_t*>(vb ? ctx->stage_v.ptr : nullptr);
+  uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
+  uint8_t* av = static_cast<uint8_t*>(vb ? ctx->alt_v.ptr : nullptr);
+  const gs::RadixJob base = [&] {
+    gs::RadixJob j = radix_job(ctx, kb, kk, vb, vk, n, flags);
+    j.status = static_cast<uint64_t*>(ctx->status.ptr);
+    return j;
+  }();
+  ctx->inject_stall = 0;
+  const uint32_t digits = uint32_t(kb + (base.ties_by_value ? vb : 0));
+
+  // Upsweep across the link; histograms back to the host.
+  gs::RadixJob up = base;
+  up.keys_in = mk;
+  up.vals_in = mv;
+  up.keys_copy = sk;
+  up.vals_copy = sv;
+  up.upsweep_only = true;
+  up.hist_copy = ctx->h_hist;
+  up.hist_ready = ctx->ev_hist;
+  up.inject_stall = 0;
+  cudaError_t e = gs::launch_radix_sort(up, ctx->props, &ctx->gen, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "upsweep launch");
+  phase_mark(ctx, "Transfer in");
+  e = cudaEventSynchronize(ctx->ev_hist);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "histograms");
+
+  // Split digit: the most significant one whose keys do not all share a bin
+  // (all above it are constant). Every element equal: the top digit.
+  uint32_t t = digits - 1;
+  for (uint32_t q = digits; q-- > 0;) {
+    const uint32_t* h = ctx->h_hist + size_t(q) * gs::RADIX;
+    if (!std::any_of(h, h + gs::RADIX, [&](uint32_t c) { return uint64_t(c) == n; })) {
+      t = q;
+      break;
+    }
+  }
+  gs::RadixJob sp = base;
+  sp.keys_in = sk;
+  sp.vals_in = sv;
+  sp.keys_out = ak;
+  sp.vals_out = av;
+  sp.keys_alt = ak;
+  sp.vals_alt = av;
+  sp.skip_upsweep = true;
+  sp.digit_lo = t;
+  sp.digit_hi = t + 1;
+  e = gs::launch_radix_sort(sp, ctx->props, &ctx->gen, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "split pass launch");
+  phase_mark(ctx, "Split");
+
+  // Each run sorts its scratch range on digits [0, hi). With an odd digit
+  // count it writes its stage range, the scratch range serving as the
+  // alternate buffer; with an even count it sorts in place in scratch with
+  // the stage range as the alternate (the plan keeps the pass count's
+  // parity, running a digit that needs no reordering as a copy if it must).
+  const auto runs = bucket_groups(ctx->h_hist + size_t(t) * gs::RADIX, n, groups);
+  auto fail_after_copies = [&](cudaError_t err, const char* where) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    return cuda_fail(ctx, err, where);
+  };
+  for (const BucketRun& r : runs) {
+    const uint64_t b = r.begin, m = r.end - r.begin;
+    const uint32_t hi = r.mixed ? t + 1 : t;
+    const uint8_t* res_k = sk + b * kb;  // where the sorted run ends up
+    const uint8_t* res_v = vb ? sv + b * vb : nullptr;
+    e = cudaSuccess;
+    if (hi == 0) {
+      // One bucket of the lowest digit, every higher digit constant: the
+      // split pass already left the run in order.
+      res_k = ak + b * kb;
+      res_v = vb ? av + b * vb : nullptr;
+    } else if (vb == 0 && m <= gs::small_sort_max()) {
+      e = gs::launch_small_sort(ak + b * kb, sk + b * kb, uint32_t(m), kb, kk, base.desc,
+                                ctx->stream);
+    } else {
+      gs::RadixJob g = base;
+      g.n = m;
+      g.keys_in = ak + b * kb;
+      if (hi & 1u) {
+        g.keys_out = sk + b * kb;
+        g.keys_alt = ak + b * kb;
+        g.alt_is_in = true;
+      } else {
+        g.keys_out = ak + b * kb;
+        g.keys_alt = sk + b * kb;
+        res_k = ak + b * kb;
+      }
+      if (vb) {
+        g.vals_in = av + b * vb;
+        g.vals_out = (hi & 1u) ? sv + b * vb : av + b * vb;
+        g.vals_alt = (hi & 1u) ? av + b * vb : sv + b * vb;
+        res_v = static_cast<const uint8_t*>(g.vals_out);
+      }
+      g.digit_lo = 0;
+      g.digit_hi = hi;
+      g.reverse_first = false;  // the split pass took care of the reversal
+      g.inject_stall = 0;
+      g.shape = pass_shape_for(ctx, kb, kk, vb, m);
+      e = gs::launch_radix_sort(g, ctx->props, &ctx->gen, ctx->stream);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_group, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_group, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<uint8_t*>(kout) + b * kb, res_k, m * kb,
+                          cudaMemcpyDeviceToHost, ctx->copy_stream);
+    if (e == cudaSuccess && vb)
+      e = cudaMemcpyAsync(static_cast<uint8_t*>(vout) + b * vb, res_v, m * vb,
+                          cudaMemcpyDeviceToHost, ctx->copy_stream);
+    if (e != cudaSuccess) return fail_after_copies(e, "bucket run launch");
+  }
+  e = cudaEventRecord(ctx->ev_copied, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0);
+  if (e != cudaSuccess) return fail_after_copies(e, "copy join");
+  phase_mark(ctx, "Sort and transfer out");
+  return check_err_word(ctx);
+}
+
 // Strategy selection: SampleSort / HykSort shapes for keys, radix otherwise
 // (every strategy gives the same bytes).
 gs_status dispatch_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, const void* kin,
@@ -609,11 +818,15 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
     const bool radix_path = has_v || n < 4096 || (algo != GS_ALGO_SAMPLE && algo != GS_ALGO_HYK);
     const void* mk = mapped_host(kin);
     const void* mv = has_v ? mapped_host(vin) : nullptr;
+    const uint32_t groups = host_groups_for(ctx, n);
+    if (radix_path && mk && (!has_v || mv) && groups > 1 && mapped_host(kout) &&
+        (!has_v || mapped_host(vout))) {
+      return host_groups_sort(ctx, kb, kk, vb, vk, mk, mv, kout, vout, n, flags, groups);
+    }
     if (radix_path && mk && (!has_v || mv)) {
       HostFuse fu;
       fu.keys_copy = ctx->stage_k.ptr;
       fu.vals_copy = has_v ? ctx->stage_v.ptr : nullptr;
-      if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
       st = device_sort(ctx, kb, kk, vb, vk, mk, mv, ctx->stage_k.ptr,
                        has_v ? ctx->stage_v.ptr : nullptr, n, flags, &fu);
       if (st != GS_OK) return st;
@@ -624,11 +837,10 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
       phase_mark(ctx, "Transfer out");
       return check_err_word(ctx);
     }
-    if (ctx->timing) cudaEventRecord(ctx->ev[0], ctx->stream);
     e = link_copy(ctx, ctx->stage_k.ptr, kin, uint64_t(n) * kb, true);
     if (e == cudaSuccess && has_v) e = link_copy(ctx, ctx->stage_v.ptr, vin, uint64_t(n) * vb, true);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "host to device copy");
-    if (ctx->timing) { ctx->n_phases = 0; phase_mark(ctx, "Transfer in"); }
+    phase_mark(ctx, "Transfer in");
     st = dispatch_sort(ctx, kb, kk, vb, vk, ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr,
                        ctx->stage_k.ptr, has_v ? ctx->stage_v.ptr : nullptr, n, flags, opts);
     if (st != GS_OK) return st;
@@ -640,7 +852,6 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
     return check_err_word(ctx);
   }
 
-  if (ctx->timing) { cudaEventRecord(ctx->ev[0], ctx->stream); }
   gs_status st = dispatch_sort(ctx, kb, kk, vb, vk, kin, has_v ? vin : nullptr, kout,
                                has_v ? vout : nullptr, n, flags, opts);
   if (st != GS_OK) return st;
@@ -741,6 +952,12 @@ void gs_ctx_destroy(gs_ctx* ctx) {
   if (ctx->err) cudaFree(ctx->err);
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->kev) if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : {ctx->ev_hist, ctx->ev_group, ctx->ev_copied}) if (ev) cudaEventDestroy(ev);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  if (ctx->h_hist) cudaFreeHost(ctx->h_hist);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -1016,6 +1233,11 @@ gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value) {
       if (value == ~0ull) { ctx->shape = -1; return GS_OK; }
       if (value >= uint64_t(gs::radix_num_shapes())) return fail(ctx, GS_ERR_INVALID, "bad shape");
       ctx->shape = int(value);
+      return GS_OK;
+    case GS_DEBUG_HOST_GROUPS:  // UINT64_MAX restores the choice by size
+      if (value == ~0ull) { ctx->host_groups = -1; return GS_OK; }
+      if (value > 256) return fail(ctx, GS_ERR_INVALID, "at most 256 groups");
+      ctx->host_groups = int(value);
       return GS_OK;
   }
   return fail(ctx, GS_ERR_INVALID, "unknown debug key");

@@ -50,7 +50,29 @@ struct RadixJob {
   // the copies, so the input crosses the CPU-GPU link once.
   void* keys_copy = nullptr;
   void* vals_copy = nullptr;
+  // Digit range [digit_lo, digit_hi) of the digit sequence (value digits
+  // first when ties go by value) that the passes sort; digit_hi 0 means
+  // every digit. The elements must already be in order by the digits above
+  // the range (a run of buckets of a split by a higher digit).
+  uint32_t digit_lo = 0, digit_hi = 0;
+  // keys_alt (and vals_alt) is keys_in (vals_in): the first pass that runs
+  // must write keys_out, so the plan makes the pass count odd. The range
+  // must hold an odd number of digits.
+  bool alt_is_in = false;
+  // Pipeline stages, for callers that decide between them on the host: only
+  // the zeroing and the upsweep (copying the histograms to `hist_copy`,
+  // HIST_WORDS words of host memory, and recording `hist_ready` after), or
+  // only the plan and the passes (histograms already in `work`).
+  bool upsweep_only = false;
+  bool skip_upsweep = false;
+  uint32_t* hist_copy = nullptr;
+  cudaEvent_t hist_ready = nullptr;
 };
+
+// Words of the digit histograms a RadixJob can copy out: 16 digits x 256
+// bins; row q is digit q of the sequence.
+constexpr uint32_t HIST_DIGITS = 16;
+constexpr uint32_t HIST_WORDS = HIST_DIGITS * 256;
 
 // Smallest tile (elements) of the pass kernel over all shapes: sizes the
 // look-back words.

@@ -30,22 +30,26 @@ __global__ void __launch_bounds__(256) plan_kernel(PlanParams p) {
   if (tid == 0) plan.gen_base = atomicAdd(p.gen_counter, uint32_t(MAX_DIGITS + 1));
   __syncthreads();
   if (tid == 0) {
+    const uint32_t lo = p.digit_lo, hi = p.digit_hi;
     bool exec[MAX_DIGITS];
     uint32_t m = 0;
     for (uint32_t q = 0; q < MAX_DIGITS; ++q) {
-      exec[q] = (q < p.digits) && !s_trivial[q];
+      exec[q] = (q >= lo && q < hi) && !s_trivial[q];
       m += exec[q];
     }
     // Every key equal: nothing to reorder, but a copy (or the reversal of a
     // stable descending pair sort) still has to reach the output.
     if (m == 0 && (!p.in_place || p.reverse_first)) {
-      exec[p.digits - 1] = true;
+      exec[hi - 1] = true;
       m = 1;
     }
-    // In place, the first pass may not write its own input: make the pass
-    // count even so the first pass writes the scratch buffer.
-    if (p.in_place && (m & 1u)) {
-      for (uint32_t q = 0; q < p.digits; ++q) {
+    // The first pass may not write its own input. In place, the pass count
+    // is made even so that the first pass writes the scratch buffer; with
+    // the scratch aliasing the input, odd so that it writes the output. A
+    // digit that needs no reordering is run as a copy to fix the parity.
+    const uint32_t want = p.alt_is_in ? 1u : 0u;
+    if ((p.in_place || p.alt_is_in) && (m & 1u) != want) {
+      for (uint32_t q = lo; q < hi; ++q) {
         if (!exec[q]) { exec[q] = true; ++m; break; }
       }
     }
@@ -149,7 +153,9 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   }
   if (tiles == 0) return cudaSuccess;
   (void)gen;
-  for (uint32_t q = 0; q < digits; ++q) {
+  const uint32_t qlo = job.digit_hi ? job.digit_lo : 0u;
+  const uint32_t qhi = job.digit_hi ? job.digit_hi : digits;
+  for (uint32_t q = qlo; q < qhi; ++q) {
     pa.pass = q;
     e = cudaLaunchKernelEx(&lc, kern, pa);
     if (e != cudaSuccess) return e;
@@ -158,19 +164,14 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   return cudaGetLastError();
 }
 
-template <typename K, typename V, int S>
-cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
-                cudaStream_t stream) {
+// Zero the histograms and count every digit of the job's elements in one
+// read (copying them on the way when keys_copy is set).
+template <typename K, typename V>
+cudaError_t launch_upsweep(const RadixJob& job, uint32_t vd, const DeviceProps& props,
+                           cudaStream_t stream) {
   constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
-  const uint32_t kd = Bits<K>::DIGITS;
-  uint32_t vd = 0;
-  if constexpr (HAS_V) vd = job.ties_by_value ? Bits<V>::DIGITS : 0;
-  const uint32_t digits = kd + vd;
-
-  if (job.marks) cudaEventRecord(job.marks[0], stream);
   cudaError_t e = cudaMemsetAsync(job.work, 0, sizeof(uint32_t) * MAX_DIGITS * RADIX, stream);
   if (e != cudaSuccess) return e;
-
   UpsweepParams up{};
   up.keys = job.keys_in;
   up.vals = job.vals_in;
@@ -198,7 +199,37 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   if (ublocks > umax) ublocks = umax;
   if (ublocks == 0) ublocks = 1;
   ukern<<<unsigned(ublocks), UPSWEEP_THREADS, usmem, stream>>>(up);
-  if (job.marks) cudaEventRecord(job.marks[1], stream);
+  return cudaGetLastError();
+}
+
+template <typename K, typename V, int S>
+cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
+                cudaStream_t stream) {
+  constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
+  const uint32_t kd = Bits<K>::DIGITS;
+  uint32_t vd = 0;
+  if constexpr (HAS_V) vd = job.ties_by_value ? Bits<V>::DIGITS : 0;
+  const uint32_t digits = kd + vd;
+
+  static_assert(MAX_DIGITS == HIST_DIGITS && RADIX == 256, "histogram copy layout");
+  if (job.digit_hi && (job.digit_hi > digits || job.digit_lo >= job.digit_hi ||
+                       (job.alt_is_in && ((job.digit_hi - job.digit_lo) & 1u) == 0)))
+    return cudaErrorInvalidValue;
+  if (job.alt_is_in && !job.digit_hi && (digits & 1u) == 0) return cudaErrorInvalidValue;
+  if (job.marks) cudaEventRecord(job.marks[0], stream);
+  cudaError_t e = cudaSuccess;
+  if (!job.skip_upsweep) {
+    e = launch_upsweep<K, V>(job, vd, props, stream);
+    if (e != cudaSuccess) return e;
+    if (job.marks) cudaEventRecord(job.marks[1], stream);
+    if (job.hist_copy) {
+      e = cudaMemcpyAsync(job.hist_copy, &job.work->hist[0][0], sizeof(uint32_t) * HIST_WORDS,
+                          cudaMemcpyDeviceToHost, stream);
+      if (e != cudaSuccess) return e;
+      if (job.hist_ready) cudaEventRecord(job.hist_ready, stream);
+    }
+    if (job.upsweep_only) return cudaSuccess;
+  }
 
   // With copies, the passes read the copies.
   RadixJob pj = job;
@@ -213,6 +244,9 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   pp.in_place = (pj.keys_in == pj.keys_out) ||
                 (HAS_V && pj.vals_in == pj.vals_out);
   pp.reverse_first = job.reverse_first;
+  pp.digit_lo = job.digit_hi ? job.digit_lo : 0u;
+  pp.digit_hi = job.digit_hi ? job.digit_hi : digits;
+  pp.alt_is_in = job.alt_is_in;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
   plan_kernel<<<1, 256, 0, stream>>>(pp);
   if (job.marks) cudaEventRecord(job.marks[2], stream);
@@ -270,6 +304,8 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.n = job.n;
   pp.digits = 1;
   pp.in_place = 0;
+  pp.digit_lo = 0;
+  pp.digit_hi = 1;
   plan_kernel<<<1, 256, 0, st>>>(pp);
   auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, 1, true>;
   cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM_BUCKET);

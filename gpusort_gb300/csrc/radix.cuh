@@ -40,6 +40,9 @@ struct OrderXform {
       : fmask(kind == KIND_FLOAT ? ~U(0) : U(0)),
         smask(kind == KIND_UNSIGNED ? U(0) : Bits<U>::SIGN),
         dmask(desc ? ~U(0) : U(0)) {}
+  // Order bits of -0.0 and +0.0 (both 0 for integer kinds).
+  __device__ __forceinline__ U neg_zero() const { return fmask ? fwd(Bits<U>::SIGN) : U(0); }
+  __device__ __forceinline__ U pos_zero() const { return fmask ? fwd(U(0)) : U(0); }
   __device__ __forceinline__ U fwd(U x) const {
     using S = typename std::make_signed<U>::type;
     const U neg = U(S(x) >> (8 * sizeof(U) - 1));
@@ -90,10 +93,17 @@ upsweep_kernel(UpsweepParams p) {
   K* const copy_k = static_cast<K*>(p.copy_keys);
   V* copy_v = nullptr;
   if constexpr (HAS_V) copy_v = static_cast<V*>(p.copy_vals);
+  // Pair sorts: -0.0 counts as +0.0 (see pass_kernel).
+  K zneg = 0, zpos = 0;
+  if (HAS_V && p.key_kind == KIND_FLOAT) {
+    zneg = order_bits<K>(Bits<K>::SIGN, p.key_kind, desc);
+    zpos = order_bits<K>(K(0), p.key_kind, desc);
+  }
   auto count = [&](const K (&k)[UNROLL], const bool (&valid)[UNROLL]) {
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      const K b = order_bits<K>(k[u], p.key_kind, desc);
+      K b = order_bits<K>(k[u], p.key_kind, desc);
+      if constexpr (HAS_V) b = b == zneg ? zpos : b;
 #pragma unroll
       for (int d = 0; d < KD; ++d) {
         const uint32_t bin = uint32_t(b >> (RADIX_BITS * d)) & (RADIX - 1);
@@ -348,8 +358,18 @@ pass_kernel(PassParams p) {
     for (uint32_t i = tid; i < nsplit; i += THREADS) s_split[i] = static_cast<const K*>(p.splitters)[i];
     __syncthreads();
   }
+  // Pair sorts order keys as std::less does, under which -0.0 and +0.0 are
+  // equal: the digits of -0.0 are taken from +0.0, so the two tie by value
+  // (or input order). Keys themselves keep their bits. Keys-only sorts put
+  // -0.0 first, one of the orders std::less allows.
+  K zneg = 0, zpos = 0;
+  if constexpr (HAS_V) {
+    zneg = kx.neg_zero();
+    zpos = kx.pos_zero();
+  }
   // Digit of order bits: a radix digit, or the bucket (upper_bound).
   auto key_digit = [&](K y) -> uint32_t {
+    if constexpr (HAS_V) y = y == zneg ? zpos : y;
     if constexpr (!BUCKET) return uint32_t(y >> shift) & (RADIX - 1);
     return bucket_of(s_split, nsplit, y);
   };

@@ -40,6 +40,8 @@ struct PlanParams {
   uint32_t digits;        // val_digits + key_digits
   uint32_t in_place;      // an output aliases its input
   uint32_t reverse_first; // first pass reads the input back to front
+  uint32_t digit_lo, digit_hi;  // digits that may run: [digit_lo, digit_hi)
+  uint32_t alt_is_in;     // scratch aliases the input: the pass count must be odd
 };
 
 struct PassParams {

@@ -206,12 +206,18 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
  * limit and the call reports GS_ERR_TIMEOUT.
  * GS_DEBUG_BUDGET: replace the HBM budget (bytes).
  * GS_DEBUG_PASS_SHAPE: tile shape of the radix pass kernel (threads x items
- * per thread x blocks per SM); the autotuner sets it. */
+ * per thread x blocks per SM); the autotuner sets it.
+ * GS_DEBUG_HOST_GROUPS: bucket groups of a GS_FLAG_HOST radix sort with
+ * pinned buffers on both ends: sorted groups leave for the host while the
+ * next group sorts. 0 or 1: sort everything, then copy out; UINT64_MAX
+ * (default): by size (16 from 2^28 elements, 8 from 2^26, 4 from 2^25,
+ * none below). */
 #define GS_DEBUG_SPIN_LIMIT   1
 #define GS_DEBUG_INJECT_STALL 2
 #define GS_DEBUG_BUDGET       3
 #define GS_DEBUG_PASS_SHAPE   4  /* pass-kernel tile shape 0..2 (tuning);
                                     UINT64_MAX: per-type default */
+#define GS_DEBUG_HOST_GROUPS  5  /* 0..256; UINT64_MAX: by size */
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
 /* ---- Tuning table (autotuner output) ----

@@ -12,7 +12,8 @@
 //    94-145 local sort + SortAmongProcesses 453-536; include/omp/
 //    omp_utils.h:147-207 MergeSort; include/common.h:156-164 ConvertComp).
 //    A sorted multiset is unique, so std::sort reproduces it bit for bit
-//    (given no NaN; -0.0 and +0.0 compare equal, so inputs avoid -0.0).
+//    (given no NaN; -0.0 and +0.0 compare equal, so keys-only inputs avoid
+//    -0.0, and pair inputs holding both zeros have distinct values).
 //
 //  * oracle_sort_pairs: the CPU key/value path sorts std::pair<K,V> with
 //    ConvertComp<pair>(comp), i.e. lexicographic (key, value) order, both

@@ -118,6 +118,34 @@ def test_pairs(ctx, kt, vt, stable):
                 assert same_bits(gk, wk) and same_bits(gv, wv), (kt, vt, n, dist, desc, stable)
 
 
+@pytest.mark.parametrize("kt", [np.float32, np.float64])
+def test_signed_zero_keys(ctx, kt):
+    """std::less treats -0.0 and +0.0 as equal keys: pair sorts tie them by
+    value (or by input order when stable), as the oracle's std::pair and
+    std::stable_sort orders do; keys keep their bits. Keys-only sorts put
+    -0.0 first (an order std::less allows)."""
+    ubits = np.uint32 if kt is np.float32 else np.uint64
+    sign = ubits(1) << ubits(8 * np.dtype(kt).itemsize - 1)
+    for n in (1000, 100003):
+        rng = np.random.default_rng(n)
+        k = rng.choice(np.array([-0.0, 0.0, -1.5, 2.0, -np.inf], dtype=kt), size=n)
+        for desc in (False, True):
+            for stable in (False, True):
+                # Ties by value need distinct values: (-0.0, v) and (+0.0, v)
+                # would be equal elements with different bits.
+                v = (rng.integers(0, 64, size=n, dtype=np.uint32) if stable
+                     else rng.permutation(n).astype(np.uint32))
+                gk, gv = _pairs(ctx, k, v, desc, stable)
+                wk, wv = oracle.sort_pairs(k, v, desc, stable)
+                assert same_bits(gk, wk) and same_bits(gv, wv), (n, desc, stable)
+            got = _sort(ctx, k, desc)
+            b = got.view(ubits)
+            key = np.where(b & sign, ~b, b | sign)  # total order, -0.0 < +0.0
+            key = ~key if desc else key
+            assert np.all(key[1:] >= key[:-1])
+            assert same_bits(np.sort(got.view(ubits)), np.sort(k.view(ubits)))
+
+
 def test_pairs_stable_index_payload_large(ctx):
     """(uint64 key, uint32 original index) pairs, Zipf keys: stable order."""
     n = (1 << 21) + 3
