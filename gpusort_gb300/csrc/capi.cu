@@ -48,6 +48,7 @@ struct gs_ctx {
   DevBuf alt_k, alt_v;
   DevBuf stage_k, stage_v, stage_off;
   DevBuf splitters;  // sample sort
+  DevBuf merge_splits;  // HykSort shape: merge-path splits of one level
   // phase timing
   cudaEvent_t ev[8] = {};
   int n_phases = 0;
@@ -568,10 +569,17 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
   st = sort_segments_in_place(ctx, kb, kk, desc, out, n, off);
   if (st != GS_OK) return st;
   phase_mark(ctx, "Local sort");
+  size_t split_words = 0;  // tiles are counted per pair of full runs: any level may need the most
+  for (uint64_t r = run; r < n; r *= 2)
+    split_words = std::max(split_words, gs::merge_split_words(n, r, kb));
+  st = ensure(ctx, ctx->merge_splits, std::max<size_t>(split_words, 1) * sizeof(uint64_t));
+  if (st != GS_OK) return st;
   void* cur = out;
   void* other = ctx->alt_k.ptr;
   for (uint64_t r = run; r < n; r *= 2) {
-    cudaError_t e = gs::launch_merge_pass(cur, other, n, r, kb, kk, desc, ctx->stream);
+    cudaError_t e = gs::launch_merge_pass(cur, other, n, r, kb, kk, desc,
+                                          static_cast<uint64_t*>(ctx->merge_splits.ptr),
+                                          ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "merge launch");
     std::swap(cur, other);
   }
@@ -946,7 +954,7 @@ void gs_ctx_destroy(gs_ctx* ctx) {
   cudaSetDevice(ctx->props.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->status, &ctx->alt_k, &ctx->alt_v, &ctx->stage_k, &ctx->stage_v,
-                    &ctx->stage_off, &ctx->splitters};
+                    &ctx->stage_off, &ctx->splitters, &ctx->merge_splits};
   for (DevBuf* b : bufs) if (b->ptr) cudaFree(b->ptr);
   if (ctx->work) cudaFree(ctx->work);
   if (ctx->err) cudaFree(ctx->err);

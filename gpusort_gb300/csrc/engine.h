@@ -153,8 +153,10 @@ cudaError_t launch_bucket_pass(const RadixJob& job, const void* splitters, uint3
 
 // One level of the merge tree: merge adjacent sorted runs of length `run`
 // of `in` (n keys, order of key_kind/desc) into runs of 2*run in `out`.
+// `splits` is device scratch of merge_split_words(n, run, key_bytes) words.
+size_t merge_split_words(uint64_t n, uint64_t run, int key_bytes);
 cudaError_t launch_merge_pass(const void* in, void* out, uint64_t n, uint64_t run, int key_bytes,
-                              uint32_t key_kind, bool desc, cudaStream_t st);
+                              uint32_t key_kind, bool desc, uint64_t* splits, cudaStream_t st);
 
 // Allow `kern` up to `bytes` of dynamic shared memory on the current device
 // (once per kernel and device; safe to call from any thread).

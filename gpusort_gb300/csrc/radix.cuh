@@ -195,17 +195,41 @@ struct PassConfig {
   static constexpr size_t DYN_SMEM_BUCKET = DYN_SMEM + size_t(TILE);
 };
 
-// Number of sorted splitters s[0..nsplit) that are <= y (upper_bound), by
-// fixed power-of-two steps: every lane runs the same predicated steps, no
-// divergent branches. nsplit < 256.
+// Splitter search tree: the nsplit sorted splitters as a complete binary
+// search tree of `levels` = ceil(log2(nsplit + 1)) levels in breadth-first
+// order (node v at tree[v], children 2v and 2v + 1, v = 1 .. 2^levels - 1),
+// slots past the last splitter holding the largest key. A search is one
+// shared load, one compare and one shift-add per level, the same for every
+// lane. nsplit < 256, so tree has room for 256 entries.
+__host__ __device__ __forceinline__ uint32_t tree_levels(uint32_t nsplit) {
+  uint32_t l = 0;
+  while ((1u << l) - 1u < nsplit) ++l;
+  return l;
+}
+
+// Fill tree[1 .. 2^levels) from sorted[0 .. nsplit), by all threads of the
+// block (the caller synchronises afterwards). Node v on level L (v = 2^L +
+// j) holds in-order element (2j + 1) * 2^(levels - L - 1) - 1.
 template <typename K>
-__device__ __forceinline__ uint32_t bucket_of(const K* s, uint32_t nsplit, K y) {
-  uint32_t lo = 0;
-  for (uint32_t step = nsplit ? (1u << (31 - __clz(nsplit))) : 0u; step; step >>= 1) {
-    const uint32_t probe = lo + step;
-    if (probe <= nsplit && s[probe - 1] <= y) lo = probe;
+__device__ __forceinline__ void build_split_tree(const K* sorted, uint32_t nsplit, K* tree,
+                                                 uint32_t levels) {
+  const uint32_t nodes = (1u << levels) - 1u;
+  for (uint32_t v = threadIdx.x + 1; v <= nodes; v += blockDim.x) {
+    const uint32_t L = 31u - __clz(v);
+    const uint32_t j = v - (1u << L);
+    const uint32_t r = ((2u * j + 1u) << (levels - L - 1u)) - 1u;
+    tree[v] = r < nsplit ? sorted[r] : ~K(0);
   }
-  return lo;
+}
+
+// Number of splitters <= y (upper_bound), i.e. y's bucket among nsplit + 1.
+template <typename K>
+__device__ __forceinline__ uint32_t tree_bucket(const K* tree, uint32_t levels, uint32_t nsplit,
+                                                K y) {
+  uint32_t v = 1;
+  for (uint32_t l = 0; l < levels; ++l) v = 2u * v + (tree[v] <= y ? 1u : 0u);
+  const uint32_t b = v - (1u << levels);
+  return b < nsplit ? b : nsplit;  // padding slots equal to y == ~0 count past the end
 }
 
 
@@ -262,7 +286,7 @@ pass_kernel(PassParams p) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_seg;
   __shared__ uint32_t s_bad;  // a digit's destination range leaves the output
-  __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode
+  __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode: splitter search tree
   __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
   __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
 
@@ -354,8 +378,9 @@ pass_kernel(PassParams p) {
       tile_base >= e1 ? 0u : uint32_t(e1 - tile_base < uint64_t(TILE) ? e1 - tile_base : uint64_t(TILE));
   const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
   const uint32_t nsplit = p.nsplit;
+  const uint32_t split_levels = BUCKET ? tree_levels(nsplit) : 0u;
   if constexpr (BUCKET) {
-    for (uint32_t i = tid; i < nsplit; i += THREADS) s_split[i] = static_cast<const K*>(p.splitters)[i];
+    build_split_tree(static_cast<const K*>(p.splitters), nsplit, s_split, tree_levels(nsplit));
     __syncthreads();
   }
   // Pair sorts order keys as std::less does, under which -0.0 and +0.0 are
@@ -371,7 +396,7 @@ pass_kernel(PassParams p) {
   auto key_digit = [&](K y) -> uint32_t {
     if constexpr (HAS_V) y = y == zneg ? zpos : y;
     if constexpr (!BUCKET) return uint32_t(y >> shift) & (RADIX - 1);
-    return bucket_of(s_split, nsplit, y);
+    return tree_bucket(s_split, split_levels, nsplit, y);
   };
 
   // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order

@@ -82,20 +82,32 @@ struct BucketHistParams {
   uint32_t* hist;  // RADIX counters (digit row 0 of the work area)
 };
 
+constexpr int HIST_THREADS = 512;
+constexpr int HIST_UNROLL = 8;  // keys per thread per step: loads in flight
+
 template <typename K>
-__global__ void __launch_bounds__(512) bucket_hist_kernel(BucketHistParams p) {
-  __shared__ K s_split[RADIX];
+__global__ void __launch_bounds__(HIST_THREADS) bucket_hist_kernel(BucketHistParams p) {
+  __shared__ K s_tree[RADIX];
   __shared__ uint32_t s_h[RADIX];
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
+  const uint32_t levels = tree_levels(p.nsplit);
   for (uint32_t i = threadIdx.x; i < RADIX; i += blockDim.x) s_h[i] = 0;
-  for (uint32_t i = threadIdx.x; i < p.nsplit; i += blockDim.x)
-    s_split[i] = static_cast<const K*>(p.splitters)[i];
+  build_split_tree(static_cast<const K*>(p.splitters), p.nsplit, s_tree, levels);
   __syncthreads();
   const K* keys = static_cast<const K*>(p.keys);
-  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < p.n; i += stride) {
-    const K y = kx.fwd(keys[i]);
-    atomicAdd(&s_h[bucket_of(s_split, p.nsplit, y)], 1u);
+  constexpr uint64_t CHUNK = uint64_t(HIST_THREADS) * HIST_UNROLL;
+  for (uint64_t base = uint64_t(blockIdx.x) * CHUNK; base < p.n; base += uint64_t(gridDim.x) * CHUNK) {
+    K y[HIST_UNROLL];
+#pragma unroll
+    for (int u = 0; u < HIST_UNROLL; ++u) {
+      const uint64_t i = base + uint64_t(u) * HIST_THREADS + threadIdx.x;
+      y[u] = i < p.n ? kx.fwd(keys[i]) : K(0);
+    }
+#pragma unroll
+    for (int u = 0; u < HIST_UNROLL; ++u) {
+      const uint64_t i = base + uint64_t(u) * HIST_THREADS + threadIdx.x;
+      if (i < p.n) atomicAdd(&s_h[tree_bucket(s_tree, levels, p.nsplit, y[u])], 1u);
+    }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < RADIX; i += blockDim.x)
@@ -117,10 +129,10 @@ cudaError_t bucketing_t(const RadixJob& job, const SampleJob& sj, const DevicePr
   sample_kernel<K><<<1, SAMPLE_THREADS, dyn, st>>>(sp);
   BucketHistParams hp{job.keys_in, job.n, job.key_kind, uint32_t(job.desc), sj.splitters,
                       sj.parts - 1, &job.work->hist[0][0]};
-  uint64_t blocks = (job.n + 511) / 512;
+  uint64_t blocks = (job.n + HIST_THREADS * HIST_UNROLL - 1) / (HIST_THREADS * HIST_UNROLL);
   const uint64_t cap = uint64_t(props.num_sms) * 4;
   if (blocks > cap) blocks = cap;
-  bucket_hist_kernel<K><<<unsigned(blocks), 512, 0, st>>>(hp);
+  bucket_hist_kernel<K><<<unsigned(blocks), HIST_THREADS, 0, st>>>(hp);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_bucket_pass(job, sj.splitters, sj.parts - 1, props, st);
