@@ -476,7 +476,8 @@ gs_status sort_segments_in_place(gs_ctx* ctx, int kb, uint32_t kk, bool desc, vo
                                  uint64_t n, const std::vector<uint64_t>& off) {
   gs_seg_plan* pl = gs::seg_plan_new();
   const std::string err = gs::seg_plan_build(pl, off.data(), uint32_t(off.size() - 1), n, kb, kk,
-                                             desc, gs::radix_segmented_shape(kb));
+                                             desc,
+                                             gs::radix_segmented_shape(kb, n, uint32_t(off.size() - 1)));
   if (!err.empty()) {
     gs::seg_plan_free(pl);
     return fail(ctx, GS_ERR_OOM, err);
@@ -1011,7 +1012,7 @@ gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
   gs_seg_plan* pl = gs::seg_plan_new();
   const std::string err = gs::seg_plan_build(pl, host_offsets, nseg, n, kb, kk,
                                              (flags & GS_FLAG_DESCENDING) != 0,
-                                             gs::radix_segmented_shape(kb));
+                                             gs::radix_segmented_shape(kb, n, nseg));
   if (!err.empty()) {
     gs::seg_plan_free(pl);
     return fail(ctx, err.find("allocation") != std::string::npos ? GS_ERR_OOM : GS_ERR_INVALID,

@@ -97,7 +97,7 @@ struct SegJob {
   uint32_t total_tiles;
 };
 uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape);
-int radix_segmented_shape(int key_bytes);
+int radix_segmented_shape(int key_bytes, uint64_t n, uint32_t nseg);
 // Enqueue only the digit passes over the large segments (plan and bin
 // bases already prepared in job.work / sj.binbase).
 cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const DeviceProps& props,
