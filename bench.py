@@ -231,6 +231,19 @@ def secondary(ctx, stream, pk: dict, steps: int, warmup: int) -> dict:
             "sum_preserved": bool(torch.isclose(fo.double().sum(), f.double().sum()))}
     del f, fo
 
+    # uint32 uniform, 2^29 keys: the HykSort shape (p=4 partition sorts,
+    # then a tree of merge-path merges)
+    u = datagen.device("uniform", n, np.uint32, seed=4)
+    uo = torch.empty_like(u)
+    ms = time_steps(lambda: ok(ctx.sort_keys(u, uo, dtype=np.uint32, algo=capi.ALGO_HYK,
+                                             partitions=4, k_way=4)), stream, steps, warmup)
+    ctx.synchronize()
+    out["u32_uniform_2^29_hyksort_p4_k4"] = {
+        "gkeys_s": n / ms / 1e6, "ms": ms, "frac_36B": 36 * n / ms / 1e6 / hbm,
+        "sorted": _unsigned_sorted(uo, False),
+        "sum_preserved": int(uo.to(torch.int64).sum()) == int(u.to(torch.int64).sum())}
+    del u, uo
+
     # uint64 Zipf(1.1) keys + uint32 index, stable, 2^29 pairs
     k = datagen.device("zipf", n, np.uint64, seed=3)
     v = torch.arange(n, dtype=torch.int32, device=k.device)
