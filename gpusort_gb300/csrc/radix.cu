@@ -1,4 +1,5 @@
 // Launchers of the onesweep radix pipeline (kernels in radix.cuh).
+#include <cstddef>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -31,26 +32,34 @@ __global__ void __launch_bounds__(256) plan_kernel(PlanParams p) {
   __syncthreads();
   if (tid == 0) {
     const uint32_t lo = p.digit_lo, hi = p.digit_hi;
+    // Ties ordered by value, with the values already non-decreasing in
+    // input order: that order is the input order, so the value digits are
+    // dropped and the first pass keeps ties stable (reversed when
+    // descending, as std::greater puts larger values first).
+    const bool drop = p.drop_val_digits > 0 && p.work->val_order_break == 0;
+    plan.first_stable = drop ? 1u : 0u;
+    plan.first_reverse = (drop && p.drop_reverse) ? 1u : 0u;
     bool exec[MAX_DIGITS];
     uint32_t m = 0;
     for (uint32_t q = 0; q < MAX_DIGITS; ++q) {
-      exec[q] = (q >= lo && q < hi) && !s_trivial[q];
+      exec[q] = (q >= lo && q < hi) && !s_trivial[q] && !(drop && q < p.drop_val_digits);
       m += exec[q];
     }
     // Every key equal: nothing to reorder, but a copy (or the reversal of a
     // stable descending pair sort) still has to reach the output.
-    if (m == 0 && (!p.in_place || p.reverse_first)) {
+    if (m == 0 && (!p.in_place || p.reverse_first || plan.first_reverse)) {
       exec[hi - 1] = true;
       m = 1;
     }
     // The first pass may not write its own input. In place, the pass count
     // is made even so that the first pass writes the scratch buffer; with
     // the scratch aliasing the input, odd so that it writes the output. A
-    // digit that needs no reordering is run as a copy to fix the parity.
+    // digit that needs no reordering is run as a copy to fix the parity
+    // (key digits come in even numbers, so one exists when it is needed).
     const uint32_t want = p.alt_is_in ? 1u : 0u;
     if ((p.in_place || p.alt_is_in) && (m & 1u) != want) {
       for (uint32_t q = lo; q < hi; ++q) {
-        if (!exec[q]) { exec[q] = true; ++m; break; }
+        if (!exec[q] && s_trivial[q]) { exec[q] = true; ++m; break; }
       }
     }
     uint32_t j = 0;
@@ -170,7 +179,7 @@ template <typename K, typename V>
 cudaError_t launch_upsweep(const RadixJob& job, uint32_t vd, const DeviceProps& props,
                            cudaStream_t stream) {
   constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
-  cudaError_t e = cudaMemsetAsync(job.work, 0, sizeof(uint32_t) * MAX_DIGITS * RADIX, stream);
+  cudaError_t e = cudaMemsetAsync(job.work, 0, offsetof(SortWork, plan), stream);
   if (e != cudaSuccess) return e;
   UpsweepParams up{};
   up.keys = job.keys_in;
@@ -182,6 +191,7 @@ cudaError_t launch_upsweep(const RadixJob& job, uint32_t vd, const DeviceProps& 
   up.val_kind = job.val_kind;
   up.desc = job.desc;
   up.val_digits = vd;
+  up.check_val_order = vd > 0 ? 1u : 0u;
   up.work = job.work;
   // Histogram columns: as many (4 to 16) as fit UPSWEEP_SMEM bytes.
   const uint32_t total_digits = vd + uint32_t(sizeof(K));
@@ -247,6 +257,8 @@ cudaError_t run(const RadixJob& job, const DeviceProps& props, uint32_t* gen,
   pp.digit_lo = job.digit_hi ? job.digit_lo : 0u;
   pp.digit_hi = job.digit_hi ? job.digit_hi : digits;
   pp.alt_is_in = job.alt_is_in;
+  pp.drop_val_digits = vd;
+  pp.drop_reverse = job.desc ? 1u : 0u;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
   plan_kernel<<<1, 256, 0, stream>>>(pp);
   if (job.marks) cudaEventRecord(job.marks[2], stream);

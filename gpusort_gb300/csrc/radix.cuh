@@ -121,6 +121,22 @@ upsweep_kernel(UpsweepParams p) {
         if (copy_v && valid[u]) copy_v[idx] = v[u];
       }
       if (vd == 0) return;  // values only copied
+      if (p.check_val_order) {
+        // Each value against its successor in input order (lane 31's
+        // successor is the next warp's first element).
+        bool broken = false;
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) {
+          const uint64_t idx = base + uint64_t(u) * THREADS + threadIdx.x;
+          V nx = __shfl_down_sync(0xFFFFFFFFu, v[u], 1);
+          if ((threadIdx.x & 31) == 31 && idx + 1 < n) nx = ld_stream(vals + idx + 1);
+          if (valid[u] && idx + 1 < n &&
+              order_bits<V>(nx, p.val_kind, false) < order_bits<V>(v[u], p.val_kind, false))
+            broken = true;
+        }
+        if (__any_sync(0xFFFFFFFFu, broken) && (threadIdx.x & 31) == 0)
+          atomicOr(&p.work->val_order_break, 1u);
+      }
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const V b = order_bits<V>(v[u], p.val_kind, desc);
@@ -316,12 +332,12 @@ pass_kernel(PassParams p) {
   K* dst_k = static_cast<K*>(dst_is_out ? p.keys_out : p.keys_alt);
   VS* dst_v = nullptr;
   if constexpr (HAS_V) dst_v = static_cast<VS*>(dst_is_out ? p.vals_out : p.vals_alt);
-  const bool reverse = first && p.reverse_first;
+  const bool reverse = first && (p.reverse_first || plan.first_reverse);
   // The first pass that runs may order equal digits arbitrarily when the
   // requested order leaves no ties to preserve (keys only, or pairs ordered
   // by value too): equal digits there are either equal in every later digit
   // (identical elements) or separated by a later, stable pass.
-  const bool unstable = first && p.first_unstable;
+  const bool unstable = first && p.first_unstable && !plan.first_stable;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;

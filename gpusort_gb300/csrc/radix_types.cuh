@@ -12,11 +12,18 @@ struct SortPlan {
   uint32_t exec_index[MAX_DIGITS];        // 0..m_exec-1, or PASS_SKIPPED
   uint32_t tile_counter[MAX_DIGITS];      // tile claim counters per pass
   uint32_t binbase[MAX_DIGITS][RADIX];    // global start of each bin
+  // Set when the value digits were dropped because the values already run
+  // in order (ties by value = input order): the first pass that runs must
+  // then rank stably, and read back to front for a descending sort.
+  uint32_t first_stable;
+  uint32_t first_reverse;
 };
 
-// Scratch words of one sort: histograms (zeroed before the upsweep) + plan.
+// Scratch words of one sort: histograms and the value-order flag (zeroed
+// before the upsweep), plan.
 struct SortWork {
   uint32_t hist[MAX_DIGITS][RADIX];
+  uint32_t val_order_break;  // a value orders before its predecessor in the input
   SortPlan plan;
   uint32_t gen_counter;  // per status buffer: the next free look-back tag
 };
@@ -31,6 +38,8 @@ struct UpsweepParams {
   SortWork* work;
   void* copy_keys;        // when set: every key read is also stored here
   void* copy_vals;        // (and every value, when val_digits > 0)
+  uint32_t check_val_order;  // set work->val_order_break if the values are
+                             // not non-decreasing (std::less) in input order
 };
 
 struct PlanParams {
@@ -42,6 +51,11 @@ struct PlanParams {
   uint32_t reverse_first; // first pass reads the input back to front
   uint32_t digit_lo, digit_hi;  // digits that may run: [digit_lo, digit_hi)
   uint32_t alt_is_in;     // scratch aliases the input: the pass count must be odd
+  // Value digits 0 .. drop_val_digits-1 may be dropped when the upsweep
+  // found the values in order; the sort then keeps ties in input order
+  // (reversed when drop_reverse: descending).
+  uint32_t drop_val_digits;
+  uint32_t drop_reverse;
 };
 
 struct PassParams {

@@ -7,6 +7,7 @@
 // become a bucket histogram and one onesweep scatter pass whose digit is
 // the key's bucket. Each bucket is then sorted by the batched sort, as the
 // reference re-sorts each rank's received data (:486).
+#include <cstddef>
 #include <cstdint>
 
 #include "engine.h"
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(HIST_THREADS) bucket_hist_kernel(BucketHistPar
 template <typename K>
 cudaError_t bucketing_t(const RadixJob& job, const SampleJob& sj, const DeviceProps& props,
                         cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(job.work, 0, sizeof(uint32_t) * MAX_DIGITS * RADIX, st);
+  cudaError_t e = cudaMemsetAsync(job.work, 0, offsetof(SortWork, plan), st);
   if (e != cudaSuccess) return e;
   uint32_t padded = 1;
   while (padded < sj.samples) padded <<= 1;

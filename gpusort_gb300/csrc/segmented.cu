@@ -229,6 +229,8 @@ __global__ void seg_plan_kernel(SortWork* w, uint32_t digits, uint32_t* gen_coun
     w->plan.exec_index[t] = t < digits ? t : PASS_SKIPPED;
   }
   if (t == 0) {
+    w->plan.first_stable = 0;
+    w->plan.first_reverse = 0;
     w->plan.m_exec = digits;
     w->plan.gen_base = atomicAdd(gen_counter, uint32_t(MAX_DIGITS + 1));
   }

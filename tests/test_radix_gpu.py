@@ -118,6 +118,30 @@ def test_pairs(ctx, kt, vt, stable):
                 assert same_bits(gk, wk) and same_bits(gv, wv), (kt, vt, n, dist, desc, stable)
 
 
+@pytest.mark.parametrize("kt,vt", [(np.uint32, np.uint32), (np.int64, np.uint32),
+                                   (np.float32, np.uint64), (np.uint64, np.int64)])
+def test_pairs_values_in_order(ctx, kt, vt):
+    """Ties ordered by value when the values already run in order (an index
+    payload): the engine drops the value digits and keeps ties in input
+    order (reversed when descending). Few distinct keys make every tie
+    visible; a single out-of-order value (at a warp boundary, at a
+    4096-element chunk boundary, at the end) must switch the shortcut off."""
+    for n in (1000, 100003, (1 << 21) + 7):
+        k = datagen.host("distinct8", n, kt, seed=n)
+        base = np.arange(n, dtype=np.uint64) // 3  # non-decreasing, with runs
+        cases = [base.astype(vt)]
+        for pos in sorted({31, min(4095, n - 2), n - 2}):
+            v = base.copy()
+            v[pos], v[pos + 1] = base[pos + 1] + 1, base[pos]
+            cases.append(v.astype(vt))
+        for v in cases:
+            for desc in (False, True):
+                for in_place in (False, True):
+                    gk, gv = _pairs(ctx, k, v, desc, False, in_place=in_place)
+                    wk, wv = oracle.sort_pairs(k, v, desc, False)
+                    assert same_bits(gk, wk) and same_bits(gv, wv), (n, desc, in_place)
+
+
 @pytest.mark.parametrize("kt", [np.float32, np.float64])
 def test_signed_zero_keys(ctx, kt):
     """std::less treats -0.0 and +0.0 as equal keys: pair sorts tie them by
