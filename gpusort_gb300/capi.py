@@ -43,6 +43,7 @@ DEBUG_INJECT_STALL = 2
 DEBUG_BUDGET = 3
 DEBUG_PASS_SHAPE = 4
 DEBUG_HOST_GROUPS = 5
+DEBUG_HOST_CHUNKED = 6
 
 # Every symbol include/gpusort_gb300.h declares (checked by the CPU tests).
 EXPORTED = [

@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -61,9 +62,17 @@ struct gs_ctx {
   // Host-buffer sorts in bucket groups (made on first use): the stream the
   // sorted groups leave on, its events, and the histograms read back.
   int host_groups = -1;  // -1: by size (host_groups_for); 0 or 1: one sort, then one copy out
+  uint64_t host_chunked_min = uint64_t(1) << 28;  // keys-only host sorts this large (0: none)
+                                                  // split chunk by chunk
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_hist = nullptr, ev_group = nullptr, ev_copied = nullptr;
-  uint32_t* h_hist = nullptr;  // pinned, gs::HIST_WORDS words
+  uint32_t* h_hist = nullptr;  // pinned, gs::HIST_WORDS words per input chunk
+  // Chunked host sorts: the split stream, per-chunk events, a second work
+  // area (chunks alternate) and a third key buffer.
+  cudaStream_t split_stream = nullptr;
+  cudaEvent_t ev_chunk_in[8] = {}, ev_chunk_split[8] = {};
+  gs::SortWork* work2 = nullptr;
+  DevBuf third_k;
 };
 
 namespace gs {
@@ -592,6 +601,11 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
   return GS_OK;
 }
 
+// Chunks of a chunked host sort (host_groups_chunked). Measured on GB300
+// with pinned buffers, 16 groups: 2^30 u32 keys 44.8 ms (47.0 ms with one
+// split after the whole input); 2^28: 11.7 vs 11.9 ms; 2^27: no gain.
+constexpr uint32_t HOST_CHUNKS = 4;
+
 // Bucket groups of a host sort of n elements (below 2: not grouped).
 // Measured on GB300, 2^30 u32 keys with pinned buffers: 58.7 ms ungrouped,
 // 50.1 / 48.0 / 47.0 / 48.0 ms with 4 / 8 / 16 / 32 groups; 2^26 keys: 3.76
@@ -632,33 +646,156 @@ std::vector<BucketRun> bucket_groups(const uint32_t* counts, uint64_t n, uint32_
   return out;
 }
 
+// Host sorts in bucket groups: the stream, events and host memory they use,
+// made on first use.
+gs_status host_groups_setup(gs_ctx* ctx) {
+  if (ctx->copy_stream) return GS_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->split_stream, cudaStreamNonBlocking);
+  for (cudaEvent_t* ev : {&ctx->ev_hist, &ctx->ev_group, &ctx->ev_copied})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  for (uint32_t c = 0; c < HOST_CHUNKS && e == cudaSuccess; ++c) {
+    e = cudaEventCreateWithFlags(&ctx->ev_chunk_in[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_chunk_split[c], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess)
+    e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_hist),
+                      sizeof(uint32_t) * gs::HIST_WORDS * HOST_CHUNKS, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->work2, gs::sort_work_bytes());
+  if (e == cudaSuccess) e = cudaMemset(ctx->work2, 0, gs::sort_work_bytes());
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "host-sort stream setup");
+  ctx->held += gs::sort_work_bytes();
+  return GS_OK;
+}
+
+// The most significant digit of a histogram set (digits x 256 counts of n
+// elements) whose elements do not all share a bin; every digit above it is
+// constant. Every element equal: the top digit.
+uint32_t split_digit(const uint32_t* hist, uint32_t digits, uint64_t n) {
+  for (uint32_t q = digits; q-- > 0;) {
+    const uint32_t* h = hist + size_t(q) * gs::RADIX;
+    if (!std::any_of(h, h + gs::RADIX, [&](uint32_t c) { return uint64_t(c) == n; })) return q;
+  }
+  return digits - 1;
+}
+
+// Sort each run of buckets and copy it to the host on the copy stream while
+// the next run sorts. Each run's elements lie at [begin, end) of `in_k`
+// (and `in_v`), split by digit t; `gather` (optional) puts them there first.
+// `other_k` is free over the same range. A run of one bucket is sorted on
+// the digits below t; a run of several on the digits up to t, since LSD
+// passes on the lower digits alone would undo the split's order (the last
+// pass, on t, restores it with the lower digits as the tie order). With an
+// odd digit count a run writes its range of `other`, its own range serving
+// as the alternate buffer; with an even count it sorts in place with
+// `other` as the alternate (the plan keeps the pass count's parity, running
+// a digit that needs no reordering as a copy if it must).
+gs_status host_runs(gs_ctx* ctx, const gs::RadixJob& base, uint32_t t,
+                    const std::vector<BucketRun>& runs, uint8_t* in_k, uint8_t* in_v,
+                    uint8_t* other_k, uint8_t* other_v, void* kout, void* vout,
+                    const std::function<cudaError_t(const BucketRun&)>& gather) {
+  const int kb = base.key_bytes, vb = base.val_bytes;
+  auto fail_after_copies = [&](cudaError_t err, const char* where) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    return cuda_fail(ctx, err, where);
+  };
+  for (const BucketRun& r : runs) {
+    const uint64_t b = r.begin, m = r.end - r.begin;
+    const uint32_t hi = r.mixed ? t + 1 : t;
+    const uint8_t* res_k = other_k + b * kb;  // where the sorted run ends up
+    const uint8_t* res_v = vb ? other_v + b * vb : nullptr;
+    cudaError_t e = gather ? gather(r) : cudaSuccess;
+    if (e != cudaSuccess) {
+    } else if (hi == 0) {
+      // One bucket of the lowest digit, every higher digit constant: the
+      // split already left the run in order.
+      res_k = in_k + b * kb;
+      res_v = vb ? in_v + b * vb : nullptr;
+    } else if (vb == 0 && m <= gs::small_sort_max()) {
+      e = gs::launch_small_sort(in_k + b * kb, other_k + b * kb, uint32_t(m), kb, base.key_kind,
+                                base.desc, ctx->stream);
+    } else {
+      gs::RadixJob g = base;
+      g.n = m;
+      g.keys_in = in_k + b * kb;
+      if (hi & 1u) {
+        g.keys_out = other_k + b * kb;
+        g.keys_alt = in_k + b * kb;
+        g.alt_is_in = true;
+      } else {
+        g.keys_out = in_k + b * kb;
+        g.keys_alt = other_k + b * kb;
+        res_k = in_k + b * kb;
+      }
+      if (vb) {
+        g.vals_in = in_v + b * vb;
+        g.vals_out = (hi & 1u) ? other_v + b * vb : in_v + b * vb;
+        g.vals_alt = (hi & 1u) ? in_v + b * vb : other_v + b * vb;
+        res_v = static_cast<const uint8_t*>(g.vals_out);
+      }
+      g.digit_lo = 0;
+      g.digit_hi = hi;
+      g.reverse_first = false;  // the split took care of the reversal
+      g.inject_stall = 0;
+      g.shape = pass_shape_for(ctx, kb, base.key_kind, vb, m);
+      e = gs::launch_radix_sort(g, ctx->props, &ctx->gen, ctx->stream);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_group, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_group, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<uint8_t*>(kout) + b * kb, res_k, m * kb,
+                          cudaMemcpyDeviceToHost, ctx->copy_stream);
+    if (e == cudaSuccess && vb)
+      e = cudaMemcpyAsync(static_cast<uint8_t*>(vout) + b * vb, res_v, m * vb,
+                          cudaMemcpyDeviceToHost, ctx->copy_stream);
+    if (e != cudaSuccess) return fail_after_copies(e, "bucket run launch");
+  }
+  cudaError_t e = cudaEventRecord(ctx->ev_copied, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0);
+  if (e != cudaSuccess) return fail_after_copies(e, "copy join");
+  phase_mark(ctx, "Sort and transfer out");
+  return check_err_word(ctx);
+}
+
+// The radix job of a host-groups sort (buffers left to the caller).
+gs::RadixJob host_base_job(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, uint64_t n,
+                           uint32_t flags) {
+  gs::RadixJob j = radix_job(ctx, kb, kk, vb, vk, n, flags);
+  j.status = static_cast<uint64_t*>(ctx->status.ptr);
+  ctx->inject_stall = 0;
+  return j;
+}
+
+// One split pass on digit t over all n elements: stage -> scratch.
+cudaError_t launch_split(gs_ctx* ctx, const gs::RadixJob& base, uint32_t t, uint8_t* sk,
+                         uint8_t* sv, uint8_t* ak, uint8_t* av) {
+  gs::RadixJob sp = base;
+  sp.keys_in = sk;
+  sp.vals_in = sv;
+  sp.keys_out = ak;
+  sp.vals_out = av;
+  sp.keys_alt = ak;
+  sp.vals_alt = av;
+  sp.skip_upsweep = true;
+  sp.digit_lo = t;
+  sp.digit_hi = t + 1;
+  return gs::launch_radix_sort(sp, ctx->props, &ctx->gen, ctx->stream);
+}
+
 // Sort of pinned host buffers in bucket groups, so that the sort overlaps
 // the transfer out. The upsweep reads the input across the CPU-GPU link
 // into the stage buffer and counts every digit; one pass on the most
 // significant digit t that varies splits the elements into its 256 buckets
-// (stage -> scratch); then runs of buckets are sorted one after another,
-// and every sorted run is copied to the host on a second stream while the
-// next run sorts. A run of one bucket is sorted on the digits below t; a
-// run of several buckets on the digits up to t, since LSD passes on the
-// lower digits alone would undo the split's order (the last pass, on t,
-// restores it with the lower digits as the tie order). The order is the one
-// device_sort gives: the split pass is stable exactly when the first pass
-// of device_sort would be (and reads back to front when that one does),
-// and each run is a whole sort on every digit that varies within it.
+// (stage -> scratch); then runs of buckets are sorted and copied out one
+// after another (host_runs). The order is the one device_sort gives: the
+// split pass is stable exactly when the first pass of device_sort would be
+// (and reads back to front when that one does), and each run is a whole
+// sort on every digit that varies within it.
 gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, const void* mk,
                            const void* mv, void* kout, void* vout, uint64_t n, uint32_t flags,
                            uint32_t groups) {
-  if (!ctx->copy_stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_hist, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_group, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming);
-    if (e == cudaSuccess)
-      e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_hist), sizeof(uint32_t) * gs::HIST_WORDS,
-                        cudaHostAllocDefault);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "host-sort stream setup");
-  }
-  gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  gs_status st = host_groups_setup(ctx);
+  if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st == GS_OK && vb) st = ensure(ctx, ctx->alt_v, size_t(n) * vb);
   if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), 0);
   if (st != GS_OK) return st;
@@ -666,12 +803,7 @@ gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk
   uint8_t* sv = static_cast<uint8_t*>(vb ? ctx->stage_v.ptr : nullptr);
   uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
   uint8_t* av = static_cast<uint8_t*>(vb ? ctx->alt_v.ptr : nullptr);
-  const gs::RadixJob base = [&] {
-    gs::RadixJob j = radix_job(ctx, kb, kk, vb, vk, n, flags);
-    j.status = static_cast<uint64_t*>(ctx->status.ptr);
-    return j;
-  }();
-  ctx->inject_stall = 0;
+  const gs::RadixJob base = host_base_job(ctx, kb, kk, vb, vk, n, flags);
   const uint32_t digits = uint32_t(kb + (base.ties_by_value ? vb : 0));
 
   // Upsweep across the link; histograms back to the host.
@@ -690,95 +822,146 @@ gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk
   e = cudaEventSynchronize(ctx->ev_hist);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "histograms");
 
-  // Split digit: the most significant one whose keys do not all share a bin
-  // (all above it are constant). Every element equal: the top digit.
-  uint32_t t = digits - 1;
-  for (uint32_t q = digits; q-- > 0;) {
-    const uint32_t* h = ctx->h_hist + size_t(q) * gs::RADIX;
-    if (!std::any_of(h, h + gs::RADIX, [&](uint32_t c) { return uint64_t(c) == n; })) {
-      t = q;
-      break;
-    }
-  }
-  gs::RadixJob sp = base;
-  sp.keys_in = sk;
-  sp.vals_in = sv;
-  sp.keys_out = ak;
-  sp.vals_out = av;
-  sp.keys_alt = ak;
-  sp.vals_alt = av;
-  sp.skip_upsweep = true;
-  sp.digit_lo = t;
-  sp.digit_hi = t + 1;
-  e = gs::launch_radix_sort(sp, ctx->props, &ctx->gen, ctx->stream);
+  const uint32_t t = split_digit(ctx->h_hist, digits, n);
+  e = launch_split(ctx, base, t, sk, sv, ak, av);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "split pass launch");
   phase_mark(ctx, "Split");
+  return host_runs(ctx, base, t, bucket_groups(ctx->h_hist + size_t(t) * gs::RADIX, n, groups),
+                   ak, av, sk, sv, kout, vout, nullptr);
+}
 
-  // Each run sorts its scratch range on digits [0, hi). With an odd digit
-  // count it writes its stage range, the scratch range serving as the
-  // alternate buffer; with an even count it sorts in place in scratch with
-  // the stage range as the alternate (the plan keeps the pass count's
-  // parity, running a digit that needs no reordering as a copy if it must).
-  const auto runs = bucket_groups(ctx->h_hist + size_t(t) * gs::RADIX, n, groups);
-  auto fail_after_copies = [&](cudaError_t err, const char* where) {
-    cudaStreamSynchronize(ctx->copy_stream);
+// Keys-only host sorts of at least 2^28 keys (by default): as
+// host_groups_sort, but the split no longer waits for the whole input. The
+// input crosses the link in HOST_CHUNKS chunks; each chunk's upsweep (one
+// CTA per SM, bound by the link) counts it and stages it, and its split on
+// the top digit into its own 256 buckets runs on a second stream while the
+// next chunk crosses the link, so only the last chunk's split is left once
+// the input is in. A run of buckets then gathers its pieces from every
+// chunk (device copies) into its stage range before it sorts, with a third
+// buffer as the alternate. Ties cannot be told apart (keys only), so the
+// chunk order of the pieces does not matter. When the top digit turns out
+// to be the same for every key, the chunk splits are of no use and the
+// single split of host_groups_sort runs on the staged input instead.
+gs_status host_groups_chunked(gs_ctx* ctx, int kb, uint32_t kk, const void* mk, void* kout,
+                              uint64_t n, uint32_t flags, uint32_t groups) {
+  gs_status st = host_groups_setup(ctx);
+  if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
+  if (st == GS_OK) st = ensure(ctx, ctx->third_k, size_t(n) * kb);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0), 0);
+  if (st != GS_OK) return st;
+  uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
+  uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
+  uint8_t* tk = static_cast<uint8_t*>(ctx->third_k.ptr);
+  const uint8_t* in = static_cast<const uint8_t*>(mk);
+  const gs::RadixJob base = host_base_job(ctx, kb, kk, 0, 0, n, flags);
+  const uint32_t digits = uint32_t(kb);
+  const uint32_t top = digits - 1;
+  // Chunk length: a multiple of 4096 keys, so every chunk starts 16-byte
+  // aligned.
+  const uint64_t len = ((n + HOST_CHUNKS - 1) / HOST_CHUNKS + 4095) & ~uint64_t(4095);
+  const uint32_t chunks = uint32_t((n + len - 1) / len);
+  cudaStream_t s1 = ctx->stream, s2 = ctx->split_stream;
+  auto fail_after_splits = [&](cudaError_t err, const char* where) {
+    cudaStreamSynchronize(s2);
     return cuda_fail(ctx, err, where);
   };
-  for (const BucketRun& r : runs) {
-    const uint64_t b = r.begin, m = r.end - r.begin;
-    const uint32_t hi = r.mixed ? t + 1 : t;
-    const uint8_t* res_k = sk + b * kb;  // where the sorted run ends up
-    const uint8_t* res_v = vb ? sv + b * vb : nullptr;
-    e = cudaSuccess;
-    if (hi == 0) {
-      // One bucket of the lowest digit, every higher digit constant: the
-      // split pass already left the run in order.
-      res_k = ak + b * kb;
-      res_v = vb ? av + b * vb : nullptr;
-    } else if (vb == 0 && m <= gs::small_sort_max()) {
-      e = gs::launch_small_sort(ak + b * kb, sk + b * kb, uint32_t(m), kb, kk, base.desc,
-                                ctx->stream);
-    } else {
-      gs::RadixJob g = base;
-      g.n = m;
-      g.keys_in = ak + b * kb;
-      if (hi & 1u) {
-        g.keys_out = sk + b * kb;
-        g.keys_alt = ak + b * kb;
-        g.alt_is_in = true;
-      } else {
-        g.keys_out = ak + b * kb;
-        g.keys_alt = sk + b * kb;
-        res_k = ak + b * kb;
-      }
-      if (vb) {
-        g.vals_in = av + b * vb;
-        g.vals_out = (hi & 1u) ? sv + b * vb : av + b * vb;
-        g.vals_alt = (hi & 1u) ? av + b * vb : sv + b * vb;
-        res_v = static_cast<const uint8_t*>(g.vals_out);
-      }
-      g.digit_lo = 0;
-      g.digit_hi = hi;
-      g.reverse_first = false;  // the split pass took care of the reversal
-      g.inject_stall = 0;
-      g.shape = pass_shape_for(ctx, kb, kk, vb, m);
-      e = gs::launch_radix_sort(g, ctx->props, &ctx->gen, ctx->stream);
-    }
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_group, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_group, 0);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(static_cast<uint8_t*>(kout) + b * kb, res_k, m * kb,
-                          cudaMemcpyDeviceToHost, ctx->copy_stream);
-    if (e == cudaSuccess && vb)
-      e = cudaMemcpyAsync(static_cast<uint8_t*>(vout) + b * vb, res_v, m * vb,
-                          cudaMemcpyDeviceToHost, ctx->copy_stream);
-    if (e != cudaSuccess) return fail_after_copies(e, "bucket run launch");
+  cudaError_t e = cudaSuccess;
+  for (uint32_t c = 0; c < chunks; ++c) {
+    const uint64_t c0 = uint64_t(c) * len, nc = std::min(len, n - c0);
+    gs::SortWork* w = (c & 1u) ? ctx->work2 : ctx->work;
+    // The chunk two back used this work area; its split must be done.
+    if (c >= 2) e = cudaStreamWaitEvent(s1, ctx->ev_chunk_split[c - 2], 0);
+    gs::RadixJob up = base;
+    up.n = nc;
+    up.keys_in = in + c0 * kb;
+    up.keys_copy = sk + c0 * kb;
+    up.work = w;
+    up.gen_counter = &ctx->work->gen_counter;  // one tag counter per status buffer
+    up.upsweep_only = true;
+    up.upsweep_per_sm = 1;
+    up.hist_copy = ctx->h_hist + size_t(c) * gs::HIST_WORDS;
+    up.inject_stall = 0;
+    if (e == cudaSuccess) e = gs::launch_radix_sort(up, ctx->props, &ctx->gen, s1);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_chunk_in[c], s1);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ctx->ev_chunk_in[c], 0);
+    gs::RadixJob sp = base;
+    sp.n = nc;
+    sp.keys_in = sk + c0 * kb;
+    sp.keys_out = ak + c0 * kb;
+    sp.keys_alt = ak + c0 * kb;
+    sp.work = w;
+    sp.gen_counter = &ctx->work->gen_counter;
+    sp.skip_upsweep = true;
+    sp.digit_lo = top;
+    sp.digit_hi = top + 1;
+    sp.inject_stall = c == 0 ? base.inject_stall : 0u;
+    if (e == cudaSuccess) e = gs::launch_radix_sort(sp, ctx->props, &ctx->gen, s2);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_chunk_split[c], s2);
+    if (e != cudaSuccess) return fail_after_splits(e, "chunk launch");
   }
-  e = cudaEventRecord(ctx->ev_copied, ctx->copy_stream);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0);
-  if (e != cudaSuccess) return fail_after_copies(e, "copy join");
-  phase_mark(ctx, "Sort and transfer out");
-  return check_err_word(ctx);
+  e = cudaEventRecord(ctx->ev_hist, s1);
+  if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_hist);
+  if (e != cudaSuccess) return fail_after_splits(e, "histograms");
+  phase_mark(ctx, "Transfer in");
+
+  // Whole-input histograms, and each chunk's bucket starts on the top digit.
+  std::vector<uint32_t> hist(gs::HIST_WORDS, 0);
+  for (uint32_t c = 0; c < chunks; ++c)
+    for (uint32_t i = 0; i < digits * gs::RADIX; ++i) hist[i] += ctx->h_hist[size_t(c) * gs::HIST_WORDS + i];
+  // All of a chunk's splits are done once the last one is.
+  e = cudaStreamWaitEvent(s1, ctx->ev_chunk_split[chunks - 1], 0);
+  if (e != cudaSuccess) return fail_after_splits(e, "split join");
+  const uint32_t t = split_digit(hist.data(), digits, n);
+  if (t != top) {
+    // The top digit is constant: split the staged input on digit t.
+    gs::RadixJob sb = base;
+    e = cudaMemcpyAsync(ctx->work->hist, hist.data(), sizeof(uint32_t) * digits * gs::RADIX,
+                        cudaMemcpyHostToDevice, s1);
+    if (e == cudaSuccess) e = launch_split(ctx, sb, t, sk, nullptr, ak, nullptr);
+    if (e != cudaSuccess) return fail_after_splits(e, "split pass launch");
+    phase_mark(ctx, "Split");
+    return host_runs(ctx, base, t, bucket_groups(hist.data() + size_t(t) * gs::RADIX, n, groups),
+                     ak, nullptr, sk, nullptr, kout, nullptr, nullptr);
+  }
+  phase_mark(ctx, "Split");
+  std::vector<uint64_t> start(size_t(chunks) * (gs::RADIX + 1));  // chunk c, bucket b
+  for (uint32_t c = 0; c < chunks; ++c) {
+    const uint32_t* h = ctx->h_hist + size_t(c) * gs::HIST_WORDS + size_t(top) * gs::RADIX;
+    uint64_t acc = 0;
+    for (uint32_t bkt = 0; bkt <= uint32_t(gs::RADIX); ++bkt) {
+      start[size_t(c) * (gs::RADIX + 1) + bkt] = acc;
+      if (bkt < uint32_t(gs::RADIX)) acc += h[bkt];
+    }
+  }
+  const auto runs = bucket_groups(hist.data() + size_t(top) * gs::RADIX, n, groups);
+  // Each run's first and last bucket, for the gather.
+  std::vector<std::pair<uint32_t, uint32_t>> span;
+  {
+    uint64_t acc = 0;
+    uint32_t bkt = 0;
+    for (const BucketRun& r : runs) {
+      while (acc < r.begin) acc += hist[size_t(top) * gs::RADIX + bkt++];
+      const uint32_t b0 = bkt;
+      while (acc < r.end) acc += hist[size_t(top) * gs::RADIX + bkt++];
+      span.emplace_back(b0, bkt);
+    }
+  }
+  size_t run_index = 0;
+  auto gather = [&](const BucketRun& r) -> cudaError_t {
+    const auto [b0, b1] = span[run_index++];
+    uint64_t dst = r.begin;
+    for (uint32_t c = 0; c < chunks; ++c) {
+      const uint64_t* cs = &start[size_t(c) * (gs::RADIX + 1)];
+      const uint64_t m = cs[b1] - cs[b0];
+      if (m == 0) continue;
+      const cudaError_t ce = cudaMemcpyAsync(sk + dst * kb, ak + (uint64_t(c) * len + cs[b0]) * kb,
+                                             m * kb, cudaMemcpyDeviceToDevice, s1);
+      if (ce != cudaSuccess) return ce;
+      dst += m;
+    }
+    return cudaSuccess;
+  };
+  return host_runs(ctx, base, top, runs, sk, nullptr, tk, nullptr, kout, nullptr, gather);
 }
 
 // Strategy selection: SampleSort / HykSort shapes for keys, radix otherwise
@@ -830,6 +1013,8 @@ gs_status sort_common(gs_ctx* ctx, gs_dtype kt, int has_v, gs_dtype vt, const vo
     const uint32_t groups = host_groups_for(ctx, n);
     if (radix_path && mk && (!has_v || mv) && groups > 1 && mapped_host(kout) &&
         (!has_v || mapped_host(vout))) {
+      if (!has_v && ctx->host_chunked_min && n >= ctx->host_chunked_min)
+        return host_groups_chunked(ctx, kb, kk, mk, kout, n, flags, groups);
       return host_groups_sort(ctx, kb, kk, vb, vk, mk, mv, kout, vout, n, flags, groups);
     }
     if (radix_path && mk && (!has_v || mv)) {
@@ -955,17 +1140,21 @@ void gs_ctx_destroy(gs_ctx* ctx) {
   cudaSetDevice(ctx->props.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->status, &ctx->alt_k, &ctx->alt_v, &ctx->stage_k, &ctx->stage_v,
-                    &ctx->stage_off, &ctx->splitters, &ctx->merge_splits};
+                    &ctx->stage_off, &ctx->splitters, &ctx->merge_splits, &ctx->third_k};
   for (DevBuf* b : bufs) if (b->ptr) cudaFree(b->ptr);
   if (ctx->work) cudaFree(ctx->work);
   if (ctx->err) cudaFree(ctx->err);
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->kev) if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : {ctx->ev_hist, ctx->ev_group, ctx->ev_copied}) if (ev) cudaEventDestroy(ev);
-  if (ctx->copy_stream) {
-    cudaStreamSynchronize(ctx->copy_stream);
-    cudaStreamDestroy(ctx->copy_stream);
+  for (cudaEvent_t ev : ctx->ev_chunk_in) if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : ctx->ev_chunk_split) if (ev) cudaEventDestroy(ev);
+  for (cudaStream_t cs : {ctx->copy_stream, ctx->split_stream}) {
+    if (!cs) continue;
+    cudaStreamSynchronize(cs);
+    cudaStreamDestroy(cs);
   }
+  if (ctx->work2) cudaFree(ctx->work2);
   if (ctx->h_hist) cudaFreeHost(ctx->h_hist);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -1243,6 +1432,7 @@ gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value) {
       if (value >= uint64_t(gs::radix_num_shapes())) return fail(ctx, GS_ERR_INVALID, "bad shape");
       ctx->shape = int(value);
       return GS_OK;
+    case GS_DEBUG_HOST_CHUNKED: ctx->host_chunked_min = value; return GS_OK;
     case GS_DEBUG_HOST_GROUPS:  // UINT64_MAX restores the choice by size
       if (value == ~0ull) { ctx->host_groups = -1; return GS_OK; }
       if (value > 256) return fail(ctx, GS_ERR_INVALID, "at most 256 groups");

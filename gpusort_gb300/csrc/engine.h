@@ -67,6 +67,10 @@ struct RadixJob {
   bool skip_upsweep = false;
   uint32_t* hist_copy = nullptr;
   cudaEvent_t hist_ready = nullptr;
+  // Upsweep CTAs per SM (0: the default, 3). One leaves room beside it for
+  // a pass running on another stream, as when the upsweep reads across the
+  // CPU-GPU link and is bound by it.
+  uint32_t upsweep_per_sm = 0;
 };
 
 // Words of the digit histograms a RadixJob can copy out: 16 digits x 256

@@ -205,7 +205,8 @@ cudaError_t launch_upsweep(const RadixJob& job, uint32_t vd, const DeviceProps& 
   if (e != cudaSuccess) return e;
   const uint64_t chunk = uint64_t(UPSWEEP_THREADS) * UPSWEEP_UNROLL;
   uint64_t ublocks = (job.n + chunk - 1) / chunk;
-  const uint64_t umax = uint64_t(props.num_sms) * UPSWEEP_PER_SM;
+  const uint64_t umax =
+      uint64_t(props.num_sms) * (job.upsweep_per_sm ? job.upsweep_per_sm : UPSWEEP_PER_SM);
   if (ublocks > umax) ublocks = umax;
   if (ublocks == 0) ublocks = 1;
   ukern<<<unsigned(ublocks), UPSWEEP_THREADS, usmem, stream>>>(up);

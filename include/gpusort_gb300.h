@@ -211,13 +211,19 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
  * pinned buffers on both ends: sorted groups leave for the host while the
  * next group sorts. 0 or 1: sort everything, then copy out; UINT64_MAX
  * (default): by size (16 from 2^28 elements, 8 from 2^26, 4 from 2^25,
- * none below). */
+ * none below).
+ * GS_DEBUG_HOST_CHUNKED: from this many keys (default 2^28; 0: never), a
+ * keys-only grouped host sort reads its input in 4 chunks and splits each
+ * while the next crosses the link. */
 #define GS_DEBUG_SPIN_LIMIT   1
 #define GS_DEBUG_INJECT_STALL 2
 #define GS_DEBUG_BUDGET       3
 #define GS_DEBUG_PASS_SHAPE   4  /* pass-kernel tile shape 0..2 (tuning);
                                     UINT64_MAX: per-type default */
 #define GS_DEBUG_HOST_GROUPS  5  /* 0..256; UINT64_MAX: by size */
+#define GS_DEBUG_HOST_CHUNKED 6  /* smallest keys-only grouped host sort
+                                    whose input is split chunk by chunk as
+                                    it arrives (default 2^28; 0: never) */
 gs_status gs_debug_set(gs_ctx* ctx, int key, uint64_t value);
 
 /* ---- Tuning table (autotuner output) ----

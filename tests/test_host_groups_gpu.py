@@ -147,3 +147,37 @@ def test_default_grouping_by_size_and_phases(gctx):
     assert list(ph) == ["Transfer in", "Split", "Sort and transfer out"]
     assert all(t > 0 for t in ph.values())
     assert same_bits(vout, oracle.sort_keys(a))
+
+
+@pytest.fixture()
+def chunked(gctx):
+    """Chunk-by-chunk splitting from 4096 keys, so 2^22-key cases take it."""
+    gctx.debug_set(capi.DEBUG_HOST_CHUNKED, 4096)
+    yield gctx
+    gctx.debug_set(capi.DEBUG_HOST_CHUNKED, 1 << 28)
+
+
+# Key ranges: the top digit varies (chunked split) or is constant (the
+# single split on the digit below, after the chunks are in).
+@pytest.mark.parametrize("bits", [None, 24, 8, 0])
+@pytest.mark.parametrize("dtype", [np.uint32, np.float32, np.int64])
+def test_chunked_split(chunked, bits, dtype):
+    if dtype is np.float32:
+        a = datagen.host("normal", N, dtype, seed=17) if bits is None else _keys(dtype, bits, 17)
+    else:
+        a = _keys(dtype, bits, seed=17)
+    for desc in (False, True):
+        want = oracle.sort_keys(a, desc)
+        for groups in (8, 256, 2):
+            got = _sort_keys(chunked, a, desc, groups)
+            assert same_bits(got, want), (bits, desc, groups)
+
+
+def test_chunked_ragged_and_repeated(chunked):
+    """Chunk lengths are multiples of 4096 keys: sizes just around that,
+    zipf keys, back-to-back calls reusing the chunk work areas."""
+    for n in (4096 * 4 + 1, 4096 * 3 + 4095, (1 << 20) + 17):
+        a = datagen.host("zipf", n, np.uint32, seed=n)
+        want = oracle.sort_keys(a)
+        for _ in range(2):
+            assert same_bits(_sort_keys(chunked, a, False, 8), want), n
