@@ -11,8 +11,11 @@ kernels one path launches:
 * segmented  - a planned batched sort of segments with log-uniform lengths
                (group sort, per-segment histograms, segmented passes)
 * gather     - gs_gather of 8-byte elements by a random permutation
-* host       - gs_sort_keys with pinned host buffers (GS_FLAG_HOST: upsweep
-               reading across the CPU-GPU link, output by copy kernel)
+* host       - gs_sort_keys with pinned host buffers (GS_FLAG_HOST): the
+               upsweep reads across the CPU-GPU link; from 2^25 keys the
+               sort runs in bucket groups copied out while the next sorts,
+               from 2^28 keys the input is split chunk by chunk as it
+               arrives
 
 Each run is synchronous and checked for GS_OK; `--runs` (default 2) lets a
 profiler skip the first run's launches.
