@@ -156,7 +156,7 @@ int pass_shape_for(const gs_ctx* ctx, int kb, uint32_t kk, int vb, uint64_t n) {
   if (ctx->shape >= 0) return ctx->shape;
   const gs_tuning_entry* e = find_tuning(ctx, kb, kk, vb, n);
   if (e && e->pass_shape >= 0) return e->pass_shape;
-  return gs::radix_default_shape(kb, vb);
+  return gs::radix_default_shape(kb, vb, n);
 }
 
 uint32_t partitions_for(const gs_ctx* ctx, int kb, uint32_t kk, uint64_t n, const gs_opts* o) {

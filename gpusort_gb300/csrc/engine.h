@@ -84,7 +84,7 @@ uint32_t radix_tile(int key_bytes, int val_bytes);
 int radix_num_shapes();
 // Threads per CTA and items per thread of a pass shape (false: no such shape).
 bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads, uint32_t* items);
-int radix_default_shape(int key_bytes, int val_bytes);
+int radix_default_shape(int key_bytes, int val_bytes, uint64_t n);
 // Look-back words of a 32-bit keys-only job run with the default shape.
 size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.

@@ -201,8 +201,10 @@ cudaError_t launch_upsweep(const RadixJob& job, uint32_t vd, const DeviceProps& 
   // 16 columns, three 512-thread CTAs per SM and 8 loads (1.05 with 8 loads,
   // 0.98 with 32, which spill); 2^29 u64 keys: 1.01 from 1.45 ms. With
   // value digits to count (and their order to check) the narrower form
-  // stays faster: 2^29 u32 + u32 by value 2.05 vs 2.63 ms.
-  if (job.upsweep_per_sm == 0 && vd == 0 && (total_digits == 4 || total_digits == 8)) {
+  // stays faster: 2^29 u32 + u32 by value 2.05 vs 2.63 ms. So does it below
+  // 2^20 keys, where zeroing and flushing 128 KB per CTA is the bulk.
+  if (job.upsweep_per_sm == 0 && vd == 0 && (total_digits == 4 || total_digits == 8) &&
+      job.n >= (uint64_t(1) << 20)) {
     auto kw = total_digits == 4
                   ? upsweep_kernel<K, V, 1024, sizeof(K) == 4 ? 16 : 8, 5>
                   : upsweep_kernel<K, V, 1024, 8, 4>;
@@ -429,11 +431,13 @@ bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads
 // the most that fit 64 registers without spilling (u32 keys 512 x 24: 2^29
 // in 9.40 ms vs 10.71 at 16 items; u64 keys 512 x 14: 26.99 vs 28.57 ms at
 // 12; u64 + u32 pairs 512 x 10: 37.7 vs 41.7 ms at 8). The clustered shape
-// is slowest everywhere.
-int radix_default_shape(int key_bytes, int val_bytes) {
+// is slowest everywhere. Up to 2^18 keys (no payload) a sort is a few tiles
+// per pass and each pass takes about one tile's latency, so the smaller
+// 256-thread tiles win: 2^16 u32 keys 52.9 vs 65.0 us, u64 86.2 vs 102.7 us;
+// equal or worse from 2^20.
+int radix_default_shape(int key_bytes, int val_bytes, uint64_t n) {
   (void)key_bytes;
-  (void)val_bytes;
-  return 0;
+  return (val_bytes == 0 && n <= (uint64_t(1) << 18)) ? 1 : 0;
 }
 
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes) {

@@ -253,7 +253,7 @@ void start(gs_server* s, Slot& sl) {
   job.status = sl.status;
   job.work = sl.work;
   job.err = sl.err;
-  job.shape = gs::radix_default_shape(r->kb, r->vb);
+  job.shape = gs::radix_default_shape(r->kb, r->vb, n);
   uint32_t gen_unused = 0;
   if (e == cudaSuccess) {
     if (!r->has_v && n <= gs::small_sort_max())  // one CTA in shared memory

@@ -23,7 +23,9 @@ def test_table_drives_the_choice(ctx):
         assert ctx.choice(np.uint32, 0, 1000) == (1, 16)
         assert ctx.choice(np.uint32, 0, 1 << 20) == (2, 128)
         assert ctx.choice(np.uint64, 4, 1 << 25)[0] == 1
-        assert ctx.choice(np.int32, 0, 1000) == (0, 64)  # no entry: defaults
+        # No entry: the defaults (the 256-thread tiles up to 2^18 keys).
+        assert ctx.choice(np.int32, 0, 1000) == (1, 64)
+        assert ctx.choice(np.int32, 0, 1 << 22) == (0, 64)
         ctx.debug_set(capi.DEBUG_PASS_SHAPE, 0)        # explicit shape wins
         assert ctx.choice(np.uint32, 0, 1000)[0] == 0
         ctx.debug_set(capi.DEBUG_PASS_SHAPE, 2**64 - 1)
@@ -37,7 +39,8 @@ def test_table_drives_the_choice(ctx):
     finally:
         ctx.set_tuning([])
         ctx.debug_set(capi.DEBUG_PASS_SHAPE, 2**64 - 1)
-    assert ctx.choice(np.uint32, 0, 1000) == (0, 64)
+    assert ctx.choice(np.uint32, 0, 1000) == (1, 64)
+    assert ctx.choice(np.uint32, 4, 1000) == (0, 64)  # pairs keep the 512-thread tiles
 
 
 def test_quick_tune_round_trip(ctx, tmp_path):
