@@ -7,7 +7,10 @@ ascending, inputs resident in HBM. A step is one full sort of the array.
 
   value        Gkeys/s of the device-resident sort (CUDA events, K steps)
   e2e          Gkeys/s through the C ABI with pinned HOST buffers
-               (gs_sort_keys + GS_FLAG_HOST: copy in, sort, copy out)
+               (gs_sort_keys + GS_FLAG_HOST: the input is read across the
+               CPU-GPU link and split chunk by chunk as it arrives, and the
+               sort runs in bucket groups copied out while the next sorts);
+               the whole output is compared with the device sort's
   roofline     dominant kernel (one onesweep pass): algorithmic bytes of one
                launch (8 B per key: read + write of a 4-byte key) over its
                average duration measured live with CUDA events on the
@@ -19,7 +22,9 @@ ascending, inputs resident in HBM. A step is one full sort of the array.
                sample of the same workload on the host cores
   secondary    the other single-GPU workloads, device-resident, CUDA events:
                2^29 float32 N(0,1) (radix, and the SampleSort shape with
-               p=64, oversampling 32); 2^29 uint64 Zipf(1.1) keys with a
+               p=64, oversampling 32); 2^29 uint32 in the HykSort shape
+               (p=4 partition sorts, merge-path merge tree); 2^29 uint64
+               Zipf(1.1) keys with a
                uint32 index payload, stable; 100,000 uint32 segments of
                log-uniform length in [16, 2^22] scaled to ~2^30 keys, one
                planned batched sort replayed from a CUDA graph
