@@ -602,9 +602,11 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
 }
 
 // Chunks of a chunked host sort (host_groups_chunked). Measured on GB300
-// with pinned buffers, 16 groups: 2^30 u32 keys 44.8 ms (47.0 ms with one
-// split after the whole input); 2^28: 11.7 vs 11.9 ms; 2^27: no gain.
-constexpr uint32_t HOST_CHUNKS = 4;
+// with pinned buffers, 2^30 u32 keys: 47.0 ms with one split after the whole
+// input; 4 chunks, 16 groups: 44.8 ms; 8 chunks, 16 / 24 groups: 44.6 /
+// 44.2 ms (the last chunk's split, left exposed, halves). 2^28: 11.7 vs
+// 11.9 ms; 2^27: no gain.
+constexpr uint32_t HOST_CHUNKS = 8;
 
 // Bucket groups of a host sort of n elements (below 2: not grouped).
 // Measured on GB300, 2^30 u32 keys with pinned buffers: 58.7 ms ungrouped,
@@ -613,6 +615,7 @@ constexpr uint32_t HOST_CHUNKS = 4;
 // path is slower (per-group launches and host round trip).
 uint32_t host_groups_for(const gs_ctx* ctx, uint64_t n) {
   if (ctx->host_groups >= 0) return n >= 4096 ? uint32_t(ctx->host_groups) : 0u;
+  if (n >= (uint64_t(1) << 29)) return 24;
   if (n >= (uint64_t(1) << 28)) return 16;
   if (n >= (uint64_t(1) << 26)) return 8;
   if (n >= (uint64_t(1) << 25)) return 4;

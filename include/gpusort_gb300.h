@@ -210,10 +210,10 @@ int gs_kernel_times(gs_ctx* ctx, double* ms, int cap);
  * GS_DEBUG_HOST_GROUPS: bucket groups of a GS_FLAG_HOST radix sort with
  * pinned buffers on both ends: sorted groups leave for the host while the
  * next group sorts. 0 or 1: sort everything, then copy out; UINT64_MAX
- * (default): by size (16 from 2^28 elements, 8 from 2^26, 4 from 2^25,
- * none below).
+ * (default): by size (24 from 2^29 elements, 16 from 2^28, 8 from 2^26, 4
+ * from 2^25, none below).
  * GS_DEBUG_HOST_CHUNKED: from this many keys (default 2^28; 0: never), a
- * keys-only grouped host sort reads its input in 4 chunks and splits each
+ * keys-only grouped host sort reads its input in 8 chunks and splits each
  * while the next crosses the link. */
 #define GS_DEBUG_SPIN_LIMIT   1
 #define GS_DEBUG_INJECT_STALL 2
