@@ -181,3 +181,23 @@ def test_chunked_ragged_and_repeated(chunked):
         want = oracle.sort_keys(a)
         for _ in range(2):
             assert same_bits(_sort_keys(chunked, a, False, 8), want), n
+
+
+@pytest.mark.parametrize("chunk_min", [0, 4096])
+def test_in_place(gctx, chunk_min):
+    """Output buffer = input buffer: every read of the input (upsweeps across
+    the link) completes before the first run is copied out."""
+    gctx.debug_set(capi.DEBUG_HOST_CHUNKED, chunk_min)
+    try:
+        for dtype, dist in ((np.uint32, "uniform"), (np.int64, "zipf")):
+            a = datagen.host(dist, N, dtype, seed=21)
+            for desc in (False, True):
+                for groups in (8, 0):
+                    gctx.debug_set(capi.DEBUG_HOST_GROUPS, groups)
+                    h, v = _pinned(a)
+                    st = gctx.sort_keys(h, h, n=N, dtype=dtype, descending=desc,
+                                        flags=capi.FLAG_HOST)
+                    assert st == capi.GS_OK, gctx.last_error()
+                    assert same_bits(v, oracle.sort_keys(a, desc)), (dtype, desc, groups)
+    finally:
+        gctx.debug_set(capi.DEBUG_HOST_CHUNKED, 1 << 28)
