@@ -15,7 +15,8 @@ from tests._util import empty_dev, from_dev, same_bits, to_dev
 pytestmark = pytest.mark.gpu
 
 DTYPES = [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64]
-SMALL = [1, 2, 3, 31, 32, 33, 255, 256, 257, 1000, 6143, 6144, 6145, 8191, 8192, 8193, 40000]
+SMALL = [1, 2, 3, 31, 32, 33, 255, 256, 257, 1000, 4095, 4096, 4097, 6143, 6144, 6145, 8191, 8192, 8193,
+         16383, 16384, 16385, 40000]
 DISTS = ["uniform", "sorted", "reverse", "equal", "distinct8", "zipf"]
 
 
