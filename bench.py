@@ -108,8 +108,15 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a while to start: wait (up to 3 s) for its
+            # first sample, so that the timed region is sampled throughout.
+            t_end = time.perf_counter() + 3.0
+            while time.perf_counter() < t_end and self.proc.poll() is None:
+                if self.path.stat().st_size > 0:
+                    break
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
