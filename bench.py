@@ -110,9 +110,9 @@ class ClockSampler:
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
-            # nvidia-smi takes a while to start: wait (up to 3 s) for its
+            # nvidia-smi takes a while to start: wait (up to 1.5 s) for its
             # first sample, so that the timed region is sampled throughout.
-            t_end = time.perf_counter() + 3.0
+            t_end = time.perf_counter() + 1.5
             while time.perf_counter() < t_end and self.proc.poll() is None:
                 if self.path.stat().st_size > 0:
                     break
