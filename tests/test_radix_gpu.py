@@ -268,3 +268,25 @@ def test_pinned_host_buffers(ctx, n, dist):
             assert same_bits(ko[off:].numpy().view(np.uint32), wk)
             assert same_bits(vo[off:].numpy().view(np.uint32), wv)
         assert same_bits(hk[off:].numpy().view(np.uint32), a)  # input untouched
+
+
+def test_random_sizes_across_dispatch_boundaries(ctx):
+    """Seeded random sizes from 1 to ~2^21 cross every size-dependent choice
+    (one-CTA sort up to 4096 keys, 256-thread tiles up to 2^18 keys, the
+    narrow upsweep below 2^20), for every key type, both orders, keys and
+    pairs in both tie orders."""
+    rng = np.random.default_rng(20261203)
+    sizes = sorted(set(int(x) for x in np.exp2(rng.uniform(0, 21, size=36)).astype(np.int64)) |
+                   {4096, 4097, (1 << 18), (1 << 18) + 1, (1 << 20) - 1, 1 << 20})
+    for j, n in enumerate(sizes):
+        kt = DTYPES[j % len(DTYPES)]
+        dist = ("uniform", "zipf", "distinct8", "reverse")[j % 4]
+        a = datagen.host(dist, n, kt, seed=j)
+        desc = bool(j & 1)
+        assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc)), (n, kt, dist, desc)
+        if n <= (1 << 20):
+            v = np.arange(n, dtype=np.uint32)[::-1].copy()
+            stable = bool(j & 2)
+            gk, gv = _pairs(ctx, a, v, desc, stable)
+            wk, wv = oracle.sort_pairs(a, v, desc, stable)
+            assert same_bits(gk, wk) and same_bits(gv, wv), (n, kt, dist, desc, stable)
