@@ -1,10 +1,12 @@
 """Single runs of each sort path on synthetic uniform keys, for profiling the
 kernels one path launches:
 
-    python -m gpusort_gb300.workloads {radix,hyk,sample,segmented,gather,host}
+    python -m gpusort_gb300.workloads {radix,pairs,hyk,sample,segmented,gather,host}
         [--log2n N] [--runs R]
 
 * radix      - gs_sort_keys, onesweep radix (upsweep, plan, passes)
+* pairs      - gs_sort_pairs, uint64 Zipf(1.1) keys with a uint32 index
+               payload, stable (8 key-and-value passes)
 * hyk        - GS_ALGO_HYK, p=4, k=4 (partition sorts, merge-path merges)
 * sample     - GS_ALGO_SAMPLE, p=64, oversample 32 (sample, bucket
                histogram, bucket scatter pass, per-bucket batched sort)
@@ -31,7 +33,8 @@ from . import capi, datagen
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("path", choices=["radix", "hyk", "sample", "segmented", "gather", "host"])
+    ap.add_argument("path", choices=["radix", "pairs", "hyk", "sample", "segmented", "gather",
+                                     "host"])
     ap.add_argument("--log2n", type=int, default=26)
     ap.add_argument("--runs", type=int, default=2)
     args = ap.parse_args(argv)
@@ -47,6 +50,14 @@ def main(argv=None):
             raise capi.GsError(st, ctx.last_error())
 
     sync = capi.FLAG_SYNC
+    if args.path == "pairs":
+        k = datagen.device("zipf", n, np.uint64, seed=3)
+        v = torch.arange(n, dtype=torch.int32, device=k.device)
+        ko, vo = torch.empty_like(k), torch.empty_like(v)
+        torch.cuda.synchronize()
+        for _ in range(args.runs):
+            ok(ctx.sort_pairs(k, v, ko, vo, key_dtype=np.uint64, val_dtype=np.uint32, stable=True,
+                              flags=sync))
     for _ in range(args.runs):
         if args.path == "radix":
             ok(ctx.sort_keys(a, o, dtype=np.uint32, flags=sync))
