@@ -1,5 +1,7 @@
 // C ABI of the engine (include/gpusort_gb300.h): contexts, scratch held
-// within an HBM budget, host staging, dispatch to the kernel launchers.
+// within an HBM budget, dispatch to the kernel launchers, gathers, timing
+// and debug settings. The tuning table is in tuning.cu, sorts of host
+// buffers in hostsort.cu.
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
@@ -10,76 +12,20 @@
 #include <vector>
 
 #include "../../include/gpusort_gb300.h"
-#include "engine.h"
+#include "context.h"
 #include "common.cuh"
-#include "radix_types.cuh"
 
 namespace {
 
 thread_local std::string g_last_global_error;
 
-struct DevBuf {
-  void* ptr = nullptr;
-  size_t bytes = 0;
-};
-
 }  // namespace
 
 namespace gs {
+
 void set_last_global_error(const std::string& msg) { g_last_global_error = msg; }
-}  // namespace gs
 
-struct gs_ctx {
-  gs::DeviceProps props;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  std::mutex mu;
-  std::string last_error;
-  uint64_t budget = 0;  // 0: no cap
-  uint64_t held = 0;
-  uint32_t gen = 0;
-  uint32_t spin_limit = 1u << 20;
-  uint32_t inject_stall = 0;
-  int shape = -1;         // pass-kernel tile shape (debug override); -1: table / default
-  std::vector<gs_tuning_entry> tuning;  // autotuner table, first match wins
-  bool timing = false;
-  gs::SortWork* work = nullptr;
-  uint32_t* err = nullptr;
-  DevBuf status;     // look-back words
-  DevBuf alt_k, alt_v;
-  DevBuf stage_k, stage_v, stage_off;
-  DevBuf splitters;  // sample sort
-  DevBuf merge_splits;  // HykSort shape: merge-path splits of one level
-  // phase timing
-  cudaEvent_t ev[8] = {};
-  int n_phases = 0;
-  const char* phase_names[8] = {};
-  double phase_ms[8] = {};
-  // kernel timing of the last radix pipeline (3 + MAX_DIGITS marks)
-  cudaEvent_t kev[3 + 16] = {};
-  int n_kev = 0;
-  uint32_t kev_exec_mask = 0;
-  // Host-buffer sorts in bucket groups (made on first use): the stream the
-  // sorted groups leave on, its events, and the histograms read back.
-  int host_groups = -1;  // -1: by size (host_groups_for); 0 or 1: one sort, then one copy out
-  uint64_t host_chunked_min = uint64_t(1) << 28;  // keys-only host sorts this large (0: none)
-                                                  // split chunk by chunk
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t ev_hist = nullptr, ev_group = nullptr, ev_copied = nullptr;
-  uint32_t* h_hist = nullptr;  // pinned, gs::HIST_WORDS words per input chunk
-  // Chunked host sorts: the split stream, per-chunk events, a second work
-  // area (chunks alternate) and a third key buffer.
-  cudaStream_t split_stream = nullptr;
-  cudaEvent_t ev_chunk_in[8] = {}, ev_chunk_split[8] = {};
-  gs::SortWork* work2 = nullptr;
-  DevBuf third_k;
-};
-
-namespace gs {
 cudaStream_t context_stream(gs_ctx* ctx) { return ctx->stream; }
-}  // namespace gs
-
-namespace {
 
 gs_status fail(gs_ctx* ctx, gs_status st, const std::string& msg) {
   if (ctx) ctx->last_error = msg; else g_last_global_error = msg;
@@ -93,7 +39,7 @@ gs_status cuda_fail(gs_ctx* ctx, cudaError_t e, const char* where) {
 }
 
 // Grow-only scratch, bounded by the context's HBM budget.
-gs_status ensure(gs_ctx* ctx, DevBuf& b, size_t bytes, bool zero = false) {
+gs_status ensure(gs_ctx* ctx, DevBuf& b, size_t bytes, bool zero) {
   if (b.bytes >= bytes) return GS_OK;
   size_t want = bytes;
   const uint64_t next_held = ctx->held - b.bytes + want;
@@ -133,173 +79,6 @@ bool dtype_info(gs_dtype t, int* bytes, uint32_t* kind) {
     case GS_F64: *bytes = 8; *kind = gs::KIND_FLOAT; return true;
   }
   return false;
-}
-
-constexpr uint64_t MAX_N = 0xFFFFFFFFull;  // 32-bit bin counters
-
-uint32_t floor_log2(uint64_t n) { return n ? 63u - uint32_t(__builtin_clzll(n)) : 0u; }
-
-// First tuning entry for (key width and kind, payload width, size).
-const gs_tuning_entry* find_tuning(const gs_ctx* ctx, int kb, uint32_t kk, int vb, uint64_t n) {
-  const uint32_t lg = floor_log2(n);
-  for (const gs_tuning_entry& e : ctx->tuning) {
-    int ekb = 0;
-    uint32_t ekk = 0;
-    if (!dtype_info(gs_dtype(e.key_dtype), &ekb, &ekk) || ekb != kb || ekk != kk) continue;
-    if (e.val_bytes != vb || lg < e.log2n_min || lg > e.log2n_max) continue;
-    return &e;
-  }
-  return nullptr;
-}
-
-int pass_shape_for(const gs_ctx* ctx, int kb, uint32_t kk, int vb, uint64_t n) {
-  if (ctx->shape >= 0) return ctx->shape;
-  const gs_tuning_entry* e = find_tuning(ctx, kb, kk, vb, n);
-  if (e && e->pass_shape >= 0) return e->pass_shape;
-  return gs::radix_default_shape(kb, vb, n);
-}
-
-uint32_t partitions_for(const gs_ctx* ctx, int kb, uint32_t kk, uint64_t n, const gs_opts* o) {
-  if (o && o->partitions) return o->partitions;
-  const gs_tuning_entry* e = find_tuning(ctx, kb, kk, 0, n);
-  if (e && e->partitions) return e->partitions;
-  return 64;
-}
-
-bool entry_valid(const gs_tuning_entry& e) {
-  int kb = 0;
-  uint32_t kk = 0;
-  return dtype_info(gs_dtype(e.key_dtype), &kb, &kk) &&
-         (e.val_bytes == 0 || e.val_bytes == 4 || e.val_bytes == 8) &&
-         e.log2n_min <= e.log2n_max && e.log2n_max <= 63 && e.pass_shape >= -1 &&
-         e.pass_shape < gs::radix_num_shapes() && e.partitions <= gs::RADIX &&
-         (e.partitions == 0 || e.partitions >= 2);
-}
-
-// Minimal JSON reader for the tuning file: any object holding "key_dtype"
-// (at any depth) is an entry; other keys and values are skipped.
-struct Json {
-  const char* p;
-  const char* e;
-  std::vector<gs_tuning_entry>* out;
-  bool ok = true;
-
-  void ws() {
-    while (p < e && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
-  }
-  bool lit(const char* w) {
-    const size_t k = std::strlen(w);
-    if (size_t(e - p) < k || std::strncmp(p, w, k) != 0) return false;
-    p += k;
-    return true;
-  }
-  bool str(std::string* s) {
-    if (p >= e || *p != '"') return false;
-    ++p;
-    while (p < e && *p != '"') {
-      if (*p == '\\') {
-        if (++p >= e) return false;
-      }
-      if (s) s->push_back(*p);
-      ++p;
-    }
-    if (p >= e) return false;
-    ++p;
-    return true;
-  }
-  bool num(double* v) {
-    char* end = nullptr;
-    const double x = std::strtod(p, &end);
-    if (end == p || end > e) return false;
-    p = end;
-    if (v) *v = x;
-    return true;
-  }
-  // value; scalars are reported through *is_num / *d / *s
-  bool value(bool* is_num, double* d, std::string* s, int depth) {
-    if (depth > 32) return false;
-    ws();
-    if (p >= e) return false;
-    if (*p == '{') return object(depth + 1);
-    if (*p == '[') {
-      ++p;
-      ws();
-      if (p < e && *p == ']') { ++p; return true; }
-      while (true) {
-        if (!value(nullptr, nullptr, nullptr, depth + 1)) return false;
-        ws();
-        if (p < e && *p == ',') { ++p; continue; }
-        if (p < e && *p == ']') { ++p; return true; }
-        return false;
-      }
-    }
-    if (*p == '"') {
-      if (is_num) *is_num = false;
-      return str(s);
-    }
-    if (lit("true") || lit("false") || lit("null")) {
-      if (is_num) *is_num = false;
-      return true;
-    }
-    if (is_num) *is_num = true;
-    return num(d);
-  }
-  bool object(int depth) {
-    ++p;  // '{'
-    gs_tuning_entry en{-1, 0, 0, 63, -1, 0};
-    bool is_entry = false, bad = false;
-    ws();
-    if (p < e && *p == '}') { ++p; return true; }
-    while (true) {
-      ws();
-      std::string key;
-      if (!str(&key)) return false;
-      ws();
-      if (p >= e || *p != ':') return false;
-      ++p;
-      bool isn = false;
-      double d = 0;
-      std::string sv;
-      if (!value(&isn, &d, &sv, depth)) return false;
-      auto as_int = [&](int64_t lo, int64_t hi, int64_t* o) {
-        if (!isn || d != double(int64_t(d)) || d < double(lo) || d > double(hi)) { bad = true; return; }
-        *o = int64_t(d);
-      };
-      int64_t v = 0;
-      if (key == "key_dtype") {
-        is_entry = true;
-        static const char* names[] = {"u32", "i32", "f32", "u64", "i64", "f64"};
-        if (isn) { as_int(0, 5, &v); en.key_dtype = int32_t(v); }
-        else {
-          en.key_dtype = -1;
-          for (int i = 0; i < 6; ++i) if (sv == names[i]) en.key_dtype = i;
-          if (en.key_dtype < 0) bad = true;
-        }
-      } else if (key == "val_bytes") { as_int(0, 8, &v); en.val_bytes = int32_t(v); }
-      else if (key == "log2n_min") { as_int(0, 63, &v); en.log2n_min = uint32_t(v); }
-      else if (key == "log2n_max") { as_int(0, 63, &v); en.log2n_max = uint32_t(v); }
-      else if (key == "pass_shape") { as_int(-1, 1 << 20, &v); en.pass_shape = int32_t(v); }
-      else if (key == "partitions") { as_int(0, 1 << 20, &v); en.partitions = uint32_t(v); }
-      ws();
-      if (p < e && *p == ',') { ++p; continue; }
-      if (p < e && *p == '}') { ++p; break; }
-      return false;
-    }
-    if (is_entry) {
-      if (bad || !entry_valid(en)) ok = false;
-      else out->push_back(en);
-    }
-    return true;
-  }
-};
-
-int parse_tuning(const char* json, std::vector<gs_tuning_entry>* out) {
-  if (!json) return -1;
-  Json j{json, json + std::strlen(json), out};
-  if (!j.value(nullptr, nullptr, nullptr, 0)) return -1;
-  j.ws();
-  if (j.p != j.e || !j.ok) return -1;
-  return int(out->size());
 }
 
 // Phase timing of one call: the start is marked before any work is
@@ -347,66 +126,6 @@ gs_status check_err_word(gs_ctx* ctx) {
   return GS_OK;
 }
 
-// Copy kernel for transfers between device memory and pinned host memory
-// that the device addresses directly (cudaHostAlloc, cudaHostRegister): the
-// SMs load and store across the CPU-GPU link. Four independent 16-byte
-// loads per thread keep enough requests in flight for the link's latency.
-__global__ void __launch_bounds__(512) link_copy_kernel(const uint8_t* __restrict__ src,
-                                                        uint8_t* __restrict__ dst,
-                                                        uint64_t bytes) {
-  const uint64_t n16 = bytes / 16;
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n16; i += 4 * stride) {
-    const uint4 a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
-    d[i] = a;
-    d[i + stride] = b;
-    d[i + 2 * stride] = c;
-    d[i + 3 * stride] = e;
-  }
-  for (; i < n16; i += stride) d[i] = s[i];
-  if (blockIdx.x == 0 && threadIdx.x < (bytes & 15u)) dst[n16 * 16 + threadIdx.x] = src[n16 * 16 + threadIdx.x];
-}
-
-// The device address of pinned, device-mapped host memory, or null.
-const void* mapped_host(const void* p) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
-
-// Host <-> device transfer on the context's stream. Pinned host memory the
-// device can address, with both ends 16-byte aligned, moves through the SMs:
-// on GB300 that sustained about 200 GB/s each way, while the copy engine
-// gave between 56 and 200 GB/s for the same buffers. Everything else goes
-// through cudaMemcpyAsync.
-cudaError_t link_copy(gs_ctx* ctx, void* dst, const void* src, uint64_t bytes, bool to_device) {
-  if (bytes == 0) return cudaSuccess;
-  const void* host = to_device ? src : dst;
-  const void* mapped = mapped_host(host);
-  const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
-  if (!mapped || !aligned)
-    return cudaMemcpyAsync(dst, src, bytes,
-                           to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, ctx->stream);
-  const uint8_t* s = static_cast<const uint8_t*>(to_device ? mapped : src);
-  uint8_t* d = static_cast<uint8_t*>(to_device ? dst : const_cast<void*>(mapped));
-  const unsigned blocks = unsigned(std::max(1, ctx->props.num_sms) * 2);
-  link_copy_kernel<<<blocks, 512, 0, ctx->stream>>>(s, d, bytes);
-  return cudaGetLastError();
-}
-
-// Device copies the upsweep makes of a host call's pinned input, which it
-// reads directly across the CPU-GPU link (see sort_common).
-struct HostFuse {
-  void* keys_copy = nullptr;
-  void* vals_copy = nullptr;
-};
-
 // The parts of a radix job that follow from the element types, the flags
 // and the context (buffers left to the caller).
 gs::RadixJob radix_job(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind, uint64_t n,
@@ -430,6 +149,21 @@ gs::RadixJob radix_job(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vki
   job.shape = pass_shape_for(ctx, kb, kkind, vb, n);
   return job;
 }
+
+}  // namespace gs
+
+using namespace gs;
+
+namespace {
+
+constexpr uint64_t MAX_N = 0xFFFFFFFFull;  // 32-bit bin counters
+
+// Device copies the upsweep makes of a host call's pinned input, which it
+// reads directly across the CPU-GPU link (see sort_common).
+struct HostFuse {
+  void* keys_copy = nullptr;
+  void* vals_copy = nullptr;
+};
 
 // Device-memory radix sort of keys or pairs.
 gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind,
@@ -599,372 +333,6 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
   }
   phase_mark(ctx, "Merge data");
   return GS_OK;
-}
-
-// Chunks of a chunked host sort (host_groups_chunked). Measured on GB300
-// with pinned buffers, 2^30 u32 keys: 47.0 ms with one split after the whole
-// input; 4 chunks, 16 groups: 44.8 ms; 8 chunks, 16 / 24 groups: 44.6 /
-// 44.2 ms (the last chunk's split, left exposed, halves). 2^28: 11.7 vs
-// 11.9 ms; 2^27: no gain.
-constexpr uint32_t HOST_CHUNKS = 8;
-
-// Bucket groups of a host sort of n elements (below 2: not grouped).
-// Measured on GB300, 2^30 u32 keys with pinned buffers: 58.7 ms ungrouped,
-// 50.1 / 48.0 / 47.0 / 48.0 ms with 4 / 8 / 16 / 32 groups; 2^26 keys: 3.76
-// ms ungrouped, 3.26 with 4 or 8 groups; at 2^24 and below the grouped
-// path is slower (per-group launches and host round trip).
-uint32_t host_groups_for(const gs_ctx* ctx, uint64_t n) {
-  if (ctx->host_groups >= 0) return n >= 4096 ? uint32_t(ctx->host_groups) : 0u;
-  if (n >= (uint64_t(1) << 29)) return 24;
-  if (n >= (uint64_t(1) << 28)) return 16;
-  if (n >= (uint64_t(1) << 26)) return 8;
-  if (n >= (uint64_t(1) << 25)) return 4;
-  return 0;
-}
-
-// A run of whole buckets: elements [begin, end), and whether more than one
-// bucket holds elements.
-struct BucketRun {
-  uint64_t begin, end;
-  bool mixed;
-};
-
-// Runs of whole buckets of `counts` (one digit's histogram, in output
-// order) holding about n / groups elements each.
-std::vector<BucketRun> bucket_groups(const uint32_t* counts, uint64_t n, uint32_t groups) {
-  std::vector<BucketRun> out;
-  uint64_t begin = 0, acc = 0;
-  uint32_t filled = 0;
-  for (uint32_t b = 0; b < gs::RADIX; ++b) {
-    acc += counts[b];
-    filled += counts[b] != 0;
-    const bool close = b + 1 == uint32_t(gs::RADIX) ||
-                       acc * groups >= (uint64_t(out.size()) + 1) * n;
-    if (close && acc > begin) {
-      out.push_back({begin, acc, filled > 1});
-      begin = acc;
-      filled = 0;
-    }
-  }
-  return out;
-}
-
-// Host sorts in bucket groups: the stream, events and host memory they use,
-// made on first use.
-gs_status host_groups_setup(gs_ctx* ctx) {
-  if (ctx->copy_stream) return GS_OK;
-  cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->split_stream, cudaStreamNonBlocking);
-  for (cudaEvent_t* ev : {&ctx->ev_hist, &ctx->ev_group, &ctx->ev_copied})
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-  for (uint32_t c = 0; c < HOST_CHUNKS && e == cudaSuccess; ++c) {
-    e = cudaEventCreateWithFlags(&ctx->ev_chunk_in[c], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_chunk_split[c], cudaEventDisableTiming);
-  }
-  if (e == cudaSuccess)
-    e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_hist),
-                      sizeof(uint32_t) * gs::HIST_WORDS * HOST_CHUNKS, cudaHostAllocDefault);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->work2, gs::sort_work_bytes());
-  if (e == cudaSuccess) e = cudaMemset(ctx->work2, 0, gs::sort_work_bytes());
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "host-sort stream setup");
-  ctx->held += gs::sort_work_bytes();
-  return GS_OK;
-}
-
-// The most significant digit of a histogram set (digits x 256 counts of n
-// elements) whose elements do not all share a bin; every digit above it is
-// constant. Every element equal: the top digit.
-uint32_t split_digit(const uint32_t* hist, uint32_t digits, uint64_t n) {
-  for (uint32_t q = digits; q-- > 0;) {
-    const uint32_t* h = hist + size_t(q) * gs::RADIX;
-    if (!std::any_of(h, h + gs::RADIX, [&](uint32_t c) { return uint64_t(c) == n; })) return q;
-  }
-  return digits - 1;
-}
-
-// Sort each run of buckets and copy it to the host on the copy stream while
-// the next run sorts. Each run's elements lie at [begin, end) of `in_k`
-// (and `in_v`), split by digit t; `gather` (optional) puts them there first.
-// `other_k` is free over the same range. A run of one bucket is sorted on
-// the digits below t; a run of several on the digits up to t, since LSD
-// passes on the lower digits alone would undo the split's order (the last
-// pass, on t, restores it with the lower digits as the tie order). With an
-// odd digit count a run writes its range of `other`, its own range serving
-// as the alternate buffer; with an even count it sorts in place with
-// `other` as the alternate (the plan keeps the pass count's parity, running
-// a digit that needs no reordering as a copy if it must).
-gs_status host_runs(gs_ctx* ctx, const gs::RadixJob& base, uint32_t t,
-                    const std::vector<BucketRun>& runs, uint8_t* in_k, uint8_t* in_v,
-                    uint8_t* other_k, uint8_t* other_v, void* kout, void* vout,
-                    const std::function<cudaError_t(const BucketRun&)>& gather) {
-  const int kb = base.key_bytes, vb = base.val_bytes;
-  auto fail_after_copies = [&](cudaError_t err, const char* where) {
-    cudaStreamSynchronize(ctx->copy_stream);
-    return cuda_fail(ctx, err, where);
-  };
-  for (const BucketRun& r : runs) {
-    const uint64_t b = r.begin, m = r.end - r.begin;
-    const uint32_t hi = r.mixed ? t + 1 : t;
-    const uint8_t* res_k = other_k + b * kb;  // where the sorted run ends up
-    const uint8_t* res_v = vb ? other_v + b * vb : nullptr;
-    cudaError_t e = gather ? gather(r) : cudaSuccess;
-    if (e != cudaSuccess) {
-    } else if (hi == 0) {
-      // One bucket of the lowest digit, every higher digit constant: the
-      // split already left the run in order.
-      res_k = in_k + b * kb;
-      res_v = vb ? in_v + b * vb : nullptr;
-    } else if (vb == 0 && m <= gs::small_sort_max()) {
-      e = gs::launch_small_sort(in_k + b * kb, other_k + b * kb, uint32_t(m), kb, base.key_kind,
-                                base.desc, ctx->stream);
-    } else {
-      gs::RadixJob g = base;
-      g.n = m;
-      g.keys_in = in_k + b * kb;
-      if (hi & 1u) {
-        g.keys_out = other_k + b * kb;
-        g.keys_alt = in_k + b * kb;
-        g.alt_is_in = true;
-      } else {
-        g.keys_out = in_k + b * kb;
-        g.keys_alt = other_k + b * kb;
-        res_k = in_k + b * kb;
-      }
-      if (vb) {
-        g.vals_in = in_v + b * vb;
-        g.vals_out = (hi & 1u) ? other_v + b * vb : in_v + b * vb;
-        g.vals_alt = (hi & 1u) ? in_v + b * vb : other_v + b * vb;
-        res_v = static_cast<const uint8_t*>(g.vals_out);
-      }
-      g.digit_lo = 0;
-      g.digit_hi = hi;
-      g.reverse_first = false;  // the split took care of the reversal
-      g.inject_stall = 0;
-      g.shape = pass_shape_for(ctx, kb, base.key_kind, vb, m);
-      e = gs::launch_radix_sort(g, ctx->props, &ctx->gen, ctx->stream);
-    }
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_group, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_group, 0);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(static_cast<uint8_t*>(kout) + b * kb, res_k, m * kb,
-                          cudaMemcpyDeviceToHost, ctx->copy_stream);
-    if (e == cudaSuccess && vb)
-      e = cudaMemcpyAsync(static_cast<uint8_t*>(vout) + b * vb, res_v, m * vb,
-                          cudaMemcpyDeviceToHost, ctx->copy_stream);
-    if (e != cudaSuccess) return fail_after_copies(e, "bucket run launch");
-  }
-  cudaError_t e = cudaEventRecord(ctx->ev_copied, ctx->copy_stream);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0);
-  if (e != cudaSuccess) return fail_after_copies(e, "copy join");
-  phase_mark(ctx, "Sort and transfer out");
-  return check_err_word(ctx);
-}
-
-// The radix job of a host-groups sort (buffers left to the caller).
-gs::RadixJob host_base_job(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, uint64_t n,
-                           uint32_t flags) {
-  gs::RadixJob j = radix_job(ctx, kb, kk, vb, vk, n, flags);
-  j.status = static_cast<uint64_t*>(ctx->status.ptr);
-  ctx->inject_stall = 0;
-  return j;
-}
-
-// One split pass on digit t over all n elements: stage -> scratch.
-cudaError_t launch_split(gs_ctx* ctx, const gs::RadixJob& base, uint32_t t, uint8_t* sk,
-                         uint8_t* sv, uint8_t* ak, uint8_t* av) {
-  gs::RadixJob sp = base;
-  sp.keys_in = sk;
-  sp.vals_in = sv;
-  sp.keys_out = ak;
-  sp.vals_out = av;
-  sp.keys_alt = ak;
-  sp.vals_alt = av;
-  sp.skip_upsweep = true;
-  sp.digit_lo = t;
-  sp.digit_hi = t + 1;
-  return gs::launch_radix_sort(sp, ctx->props, &ctx->gen, ctx->stream);
-}
-
-// Sort of pinned host buffers in bucket groups, so that the sort overlaps
-// the transfer out. The upsweep reads the input across the CPU-GPU link
-// into the stage buffer and counts every digit; one pass on the most
-// significant digit t that varies splits the elements into its 256 buckets
-// (stage -> scratch); then runs of buckets are sorted and copied out one
-// after another (host_runs). The order is the one device_sort gives: the
-// split pass is stable exactly when the first pass of device_sort would be
-// (and reads back to front when that one does), and each run is a whole
-// sort on every digit that varies within it.
-gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk, const void* mk,
-                           const void* mv, void* kout, void* vout, uint64_t n, uint32_t flags,
-                           uint32_t groups) {
-  gs_status st = host_groups_setup(ctx);
-  if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
-  if (st == GS_OK && vb) st = ensure(ctx, ctx->alt_v, size_t(n) * vb);
-  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), 0);
-  if (st != GS_OK) return st;
-  uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
-  uint8_t* sv = static_cast<uint8_t*>(vb ? ctx->stage_v.ptr : nullptr);
-  uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
-  uint8_t* av = static_cast<uint8_t*>(vb ? ctx->alt_v.ptr : nullptr);
-  const gs::RadixJob base = host_base_job(ctx, kb, kk, vb, vk, n, flags);
-  const uint32_t digits = uint32_t(kb + (base.ties_by_value ? vb : 0));
-
-  // Upsweep across the link; histograms back to the host.
-  gs::RadixJob up = base;
-  up.keys_in = mk;
-  up.vals_in = mv;
-  up.keys_copy = sk;
-  up.vals_copy = sv;
-  up.upsweep_only = true;
-  up.hist_copy = ctx->h_hist;
-  up.hist_ready = ctx->ev_hist;
-  up.inject_stall = 0;
-  cudaError_t e = gs::launch_radix_sort(up, ctx->props, &ctx->gen, ctx->stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "upsweep launch");
-  phase_mark(ctx, "Transfer in");
-  e = cudaEventSynchronize(ctx->ev_hist);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "histograms");
-
-  const uint32_t t = split_digit(ctx->h_hist, digits, n);
-  e = launch_split(ctx, base, t, sk, sv, ak, av);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "split pass launch");
-  phase_mark(ctx, "Split");
-  return host_runs(ctx, base, t, bucket_groups(ctx->h_hist + size_t(t) * gs::RADIX, n, groups),
-                   ak, av, sk, sv, kout, vout, nullptr);
-}
-
-// Keys-only host sorts of at least 2^28 keys (by default): as
-// host_groups_sort, but the split no longer waits for the whole input. The
-// input crosses the link in HOST_CHUNKS chunks; each chunk's upsweep (one
-// CTA per SM, bound by the link) counts it and stages it, and its split on
-// the top digit into its own 256 buckets runs on a second stream while the
-// next chunk crosses the link, so only the last chunk's split is left once
-// the input is in. A run of buckets then gathers its pieces from every
-// chunk (device copies) into its stage range before it sorts, with a third
-// buffer as the alternate. Ties cannot be told apart (keys only), so the
-// chunk order of the pieces does not matter. When the top digit turns out
-// to be the same for every key, the chunk splits are of no use and the
-// single split of host_groups_sort runs on the staged input instead.
-gs_status host_groups_chunked(gs_ctx* ctx, int kb, uint32_t kk, const void* mk, void* kout,
-                              uint64_t n, uint32_t flags, uint32_t groups) {
-  gs_status st = host_groups_setup(ctx);
-  if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
-  if (st == GS_OK) st = ensure(ctx, ctx->third_k, size_t(n) * kb);
-  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0), 0);
-  if (st != GS_OK) return st;
-  uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
-  uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
-  uint8_t* tk = static_cast<uint8_t*>(ctx->third_k.ptr);
-  const uint8_t* in = static_cast<const uint8_t*>(mk);
-  const gs::RadixJob base = host_base_job(ctx, kb, kk, 0, 0, n, flags);
-  const uint32_t digits = uint32_t(kb);
-  const uint32_t top = digits - 1;
-  // Chunk length: a multiple of 4096 keys, so every chunk starts 16-byte
-  // aligned.
-  const uint64_t len = ((n + HOST_CHUNKS - 1) / HOST_CHUNKS + 4095) & ~uint64_t(4095);
-  const uint32_t chunks = uint32_t((n + len - 1) / len);
-  cudaStream_t s1 = ctx->stream, s2 = ctx->split_stream;
-  auto fail_after_splits = [&](cudaError_t err, const char* where) {
-    cudaStreamSynchronize(s2);
-    return cuda_fail(ctx, err, where);
-  };
-  cudaError_t e = cudaSuccess;
-  for (uint32_t c = 0; c < chunks; ++c) {
-    const uint64_t c0 = uint64_t(c) * len, nc = std::min(len, n - c0);
-    gs::SortWork* w = (c & 1u) ? ctx->work2 : ctx->work;
-    // The chunk two back used this work area; its split must be done.
-    if (c >= 2) e = cudaStreamWaitEvent(s1, ctx->ev_chunk_split[c - 2], 0);
-    gs::RadixJob up = base;
-    up.n = nc;
-    up.keys_in = in + c0 * kb;
-    up.keys_copy = sk + c0 * kb;
-    up.work = w;
-    up.gen_counter = &ctx->work->gen_counter;  // one tag counter per status buffer
-    up.upsweep_only = true;
-    up.upsweep_per_sm = 1;
-    up.hist_copy = ctx->h_hist + size_t(c) * gs::HIST_WORDS;
-    up.inject_stall = 0;
-    if (e == cudaSuccess) e = gs::launch_radix_sort(up, ctx->props, &ctx->gen, s1);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_chunk_in[c], s1);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ctx->ev_chunk_in[c], 0);
-    gs::RadixJob sp = base;
-    sp.n = nc;
-    sp.keys_in = sk + c0 * kb;
-    sp.keys_out = ak + c0 * kb;
-    sp.keys_alt = ak + c0 * kb;
-    sp.work = w;
-    sp.gen_counter = &ctx->work->gen_counter;
-    sp.skip_upsweep = true;
-    sp.digit_lo = top;
-    sp.digit_hi = top + 1;
-    sp.inject_stall = c == 0 ? base.inject_stall : 0u;
-    if (e == cudaSuccess) e = gs::launch_radix_sort(sp, ctx->props, &ctx->gen, s2);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_chunk_split[c], s2);
-    if (e != cudaSuccess) return fail_after_splits(e, "chunk launch");
-  }
-  e = cudaEventRecord(ctx->ev_hist, s1);
-  if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev_hist);
-  if (e != cudaSuccess) return fail_after_splits(e, "histograms");
-  phase_mark(ctx, "Transfer in");
-
-  // Whole-input histograms, and each chunk's bucket starts on the top digit.
-  std::vector<uint32_t> hist(gs::HIST_WORDS, 0);
-  for (uint32_t c = 0; c < chunks; ++c)
-    for (uint32_t i = 0; i < digits * gs::RADIX; ++i) hist[i] += ctx->h_hist[size_t(c) * gs::HIST_WORDS + i];
-  // All of a chunk's splits are done once the last one is.
-  e = cudaStreamWaitEvent(s1, ctx->ev_chunk_split[chunks - 1], 0);
-  if (e != cudaSuccess) return fail_after_splits(e, "split join");
-  const uint32_t t = split_digit(hist.data(), digits, n);
-  if (t != top) {
-    // The top digit is constant: split the staged input on digit t.
-    gs::RadixJob sb = base;
-    e = cudaMemcpyAsync(ctx->work->hist, hist.data(), sizeof(uint32_t) * digits * gs::RADIX,
-                        cudaMemcpyHostToDevice, s1);
-    if (e == cudaSuccess) e = launch_split(ctx, sb, t, sk, nullptr, ak, nullptr);
-    if (e != cudaSuccess) return fail_after_splits(e, "split pass launch");
-    phase_mark(ctx, "Split");
-    return host_runs(ctx, base, t, bucket_groups(hist.data() + size_t(t) * gs::RADIX, n, groups),
-                     ak, nullptr, sk, nullptr, kout, nullptr, nullptr);
-  }
-  phase_mark(ctx, "Split");
-  std::vector<uint64_t> start(size_t(chunks) * (gs::RADIX + 1));  // chunk c, bucket b
-  for (uint32_t c = 0; c < chunks; ++c) {
-    const uint32_t* h = ctx->h_hist + size_t(c) * gs::HIST_WORDS + size_t(top) * gs::RADIX;
-    uint64_t acc = 0;
-    for (uint32_t bkt = 0; bkt <= uint32_t(gs::RADIX); ++bkt) {
-      start[size_t(c) * (gs::RADIX + 1) + bkt] = acc;
-      if (bkt < uint32_t(gs::RADIX)) acc += h[bkt];
-    }
-  }
-  const auto runs = bucket_groups(hist.data() + size_t(top) * gs::RADIX, n, groups);
-  // Each run's first and last bucket, for the gather.
-  std::vector<std::pair<uint32_t, uint32_t>> span;
-  {
-    uint64_t acc = 0;
-    uint32_t bkt = 0;
-    for (const BucketRun& r : runs) {
-      while (acc < r.begin) acc += hist[size_t(top) * gs::RADIX + bkt++];
-      const uint32_t b0 = bkt;
-      while (acc < r.end) acc += hist[size_t(top) * gs::RADIX + bkt++];
-      span.emplace_back(b0, bkt);
-    }
-  }
-  size_t run_index = 0;
-  auto gather = [&](const BucketRun& r) -> cudaError_t {
-    const auto [b0, b1] = span[run_index++];
-    uint64_t dst = r.begin;
-    for (uint32_t c = 0; c < chunks; ++c) {
-      const uint64_t* cs = &start[size_t(c) * (gs::RADIX + 1)];
-      const uint64_t m = cs[b1] - cs[b0];
-      if (m == 0) continue;
-      const cudaError_t ce = cudaMemcpyAsync(sk + dst * kb, ak + (uint64_t(c) * len + cs[b0]) * kb,
-                                             m * kb, cudaMemcpyDeviceToDevice, s1);
-      if (ce != cudaSuccess) return ce;
-      dst += m;
-    }
-    return cudaSuccess;
-  };
-  return host_runs(ctx, base, top, runs, sk, nullptr, tk, nullptr, kout, nullptr, gather);
 }
 
 // Strategy selection: SampleSort / HykSort shapes for keys, radix otherwise
@@ -1371,55 +739,6 @@ gs_status gs_pass_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* 
     return fail(nullptr, GS_ERR_INVALID, "no such pass shape");
   if (threads) *threads = t;
   if (items_per_thread) *items_per_thread = it;
-  return GS_OK;
-}
-
-gs_status gs_ctx_set_tuning(gs_ctx* ctx, const gs_tuning_entry* entries, uint32_t count) {
-  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
-  if (count && !entries) return fail(ctx, GS_ERR_INVALID, "null tuning entries");
-  for (uint32_t i = 0; i < count; ++i)
-    if (!entry_valid(entries[i])) return fail(ctx, GS_ERR_INVALID, "invalid tuning entry");
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  ctx->tuning.assign(entries, entries + count);
-  return GS_OK;
-}
-
-int gs_tuning_parse(const char* json, gs_tuning_entry* out, uint32_t capacity) {
-  std::vector<gs_tuning_entry> v;
-  const int k = parse_tuning(json, &v);
-  if (k < 0) return -1;
-  if (out && uint32_t(k) <= capacity) std::copy(v.begin(), v.end(), out);
-  return k;
-}
-
-gs_status gs_ctx_load_tuning(gs_ctx* ctx, const char* path) {
-  if (!ctx || !path) return fail(ctx, GS_ERR_INVALID, "null context or path");
-  FILE* f = std::fopen(path, "rb");
-  if (!f) return fail(ctx, GS_ERR_INVALID, std::string("cannot open tuning file ") + path);
-  std::string text;
-  char buf[4096];
-  size_t k;
-  while ((k = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, k);
-  std::fclose(f);
-  std::vector<gs_tuning_entry> v;
-  if (parse_tuning(text.c_str(), &v) < 0)
-    return fail(ctx, GS_ERR_INVALID, std::string("malformed tuning file ") + path);
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  ctx->tuning = std::move(v);
-  return GS_OK;
-}
-
-gs_status gs_ctx_choice(gs_ctx* ctx, gs_dtype key_dtype, int val_bytes, uint64_t n,
-                        int* pass_shape, uint32_t* partitions) {
-  if (!ctx) return fail(nullptr, GS_ERR_INVALID, "null context");
-  int kb = 0;
-  uint32_t kk = 0;
-  if (!dtype_info(key_dtype, &kb, &kk)) return fail(ctx, GS_ERR_BAD_DTYPE, "unknown key dtype");
-  if (val_bytes != 0 && val_bytes != 4 && val_bytes != 8)
-    return fail(ctx, GS_ERR_INVALID, "payload width must be 0, 4 or 8");
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  if (pass_shape) *pass_shape = pass_shape_for(ctx, kb, kk, val_bytes, n);
-  if (partitions) *partitions = partitions_for(ctx, kb, kk, n, nullptr);
   return GS_OK;
 }
 
