@@ -12,7 +12,11 @@
  * device and the call is asynchronous on the context's stream. With
  * GS_FLAG_HOST every pointer is host memory and the call is synchronous
  * (copy in, sort, copy out), which is how the reference's own API behaves
- * (src/cuda_utils.cu:403-445 stages host data through the device).
+ * (src/cuda_utils.cu:403-445 stages host data through the device). Pinned
+ * buffers (cudaHostAlloc, cudaHostRegister) are fastest: the device reads
+ * the input across the CPU-GPU link itself, and large radix sorts run in
+ * bucket groups that are copied out while the next group sorts (see
+ * GS_DEBUG_HOST_GROUPS). The output may be the input buffer.
  */
 #ifndef GPUSORT_GB300_H_
 #define GPUSORT_GB300_H_
