@@ -99,8 +99,7 @@ void phase_mark(gs_ctx* ctx, const char* name) {
 // generation tags unambiguous.
 // (Look-back tags are drawn on the device from work->gen_counter; a tag
 // repeats only after 2^30 passes.)
-gs_status prepare_status(gs_ctx* ctx, size_t words, uint32_t passes) {
-  (void)passes;
+gs_status prepare_status(gs_ctx* ctx, size_t words) {
   return ensure(ctx, ctx->status, words * sizeof(uint64_t), true);
 }
 
@@ -201,8 +200,7 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
     if (st != GS_OK) return st;
     job.vals_alt = ctx->alt_v.ptr;
   }
-  const uint32_t passes = uint32_t(kb + (job.ties_by_value ? vb : 0));
-  st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), passes);
+  st = prepare_status(ctx, gs::radix_status_words(n, kb, vb));
   if (st != GS_OK) return st;
   job.status = static_cast<uint64_t*>(ctx->status.ptr);
   if (ctx->timing) {
@@ -225,8 +223,8 @@ gs_status sort_segments_in_place(gs_ctx* ctx, int kb, uint32_t kk, bool desc, vo
     gs::seg_plan_free(pl);
     return fail(ctx, GS_ERR_OOM, err);
   }
-  gs_status st = prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX,
-                                uint32_t(kb));
+  gs_status st =
+      prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX);
   if (st == GS_OK) {
     cudaError_t e = gs::seg_plan_run(pl, buf, buf, ctx->alt_k.ptr,
                                      static_cast<uint64_t*>(ctx->status.ptr),
@@ -253,7 +251,7 @@ gs_status sample_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, v
   const bool desc = flags & GS_FLAG_DESCENDING;
   gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st == GS_OK) st = ensure(ctx, ctx->splitters, gs::RADIX * 8);
-  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0), 1);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0));
   if (st != GS_OK) return st;
   const void* src = in;
   if (in == out) {  // the bucket pass must not write its own input
@@ -580,8 +578,7 @@ gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
   }
   gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st == GS_OK)
-    st = prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX,
-                        uint32_t(kb));
+    st = prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX);
   if (st != GS_OK) {
     gs::seg_plan_free(pl);
     return st;

@@ -61,7 +61,6 @@ struct gs_ctx {
   // kernel timing of the last radix pipeline (3 + MAX_DIGITS marks)
   cudaEvent_t kev[3 + 16] = {};
   int n_kev = 0;
-  uint32_t kev_exec_mask = 0;
   // Host-buffer sorts in bucket groups (made on first use): the stream the
   // sorted groups leave on, its events, and the histograms read back.
   int host_groups = -1;  // -1: by size (host_groups_for); 0 or 1: one sort, then one copy out
@@ -89,7 +88,7 @@ gs_status ensure(gs_ctx* ctx, DevBuf& b, size_t bytes, bool zero = false);
 bool dtype_info(gs_dtype t, int* bytes, uint32_t* kind);
 void phase_reset(gs_ctx* ctx);
 void phase_mark(gs_ctx* ctx, const char* name);
-gs_status prepare_status(gs_ctx* ctx, size_t words, uint32_t passes);
+gs_status prepare_status(gs_ctx* ctx, size_t words);
 // Wait for the context's stream and report a device-side error word.
 gs_status check_err_word(gs_ctx* ctx);
 RadixJob radix_job(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkind, uint64_t n,

@@ -260,7 +260,7 @@ gs_status host_groups_sort(gs_ctx* ctx, int kb, uint32_t kk, int vb, uint32_t vk
   gs_status st = host_groups_setup(ctx);
   if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st == GS_OK && vb) st = ensure(ctx, ctx->alt_v, size_t(n) * vb);
-  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, vb), 0);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, vb));
   if (st != GS_OK) return st;
   uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
   uint8_t* sv = static_cast<uint8_t*>(vb ? ctx->stage_v.ptr : nullptr);
@@ -310,7 +310,7 @@ gs_status host_groups_chunked(gs_ctx* ctx, int kb, uint32_t kk, const void* mk, 
   gs_status st = host_groups_setup(ctx);
   if (st == GS_OK) st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st == GS_OK) st = ensure(ctx, ctx->third_k, size_t(n) * kb);
-  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0), 0);
+  if (st == GS_OK) st = prepare_status(ctx, gs::radix_status_words(n, kb, 0));
   if (st != GS_OK) return st;
   uint8_t* sk = static_cast<uint8_t*>(ctx->stage_k.ptr);
   uint8_t* ak = static_cast<uint8_t*>(ctx->alt_k.ptr);
