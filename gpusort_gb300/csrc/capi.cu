@@ -212,9 +212,10 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
   return GS_OK;
 }
 
-// Sort each of the given segments of `buf` in place (keys only); waits.
-gs_status sort_segments_in_place(gs_ctx* ctx, int kb, uint32_t kk, bool desc, void* buf,
-                                 uint64_t n, const std::vector<uint64_t>& off) {
+// Sort each of the given segments of `in` into `out` (keys only; `scratch`
+// holds n keys and differs from both; in == out sorts in place); waits.
+gs_status sort_segments(gs_ctx* ctx, int kb, uint32_t kk, bool desc, const void* in, void* out,
+                        void* scratch, uint64_t n, const std::vector<uint64_t>& off) {
   gs_seg_plan* pl = gs::seg_plan_new();
   const std::string err = gs::seg_plan_build(pl, off.data(), uint32_t(off.size() - 1), n, kb, kk,
                                              desc,
@@ -226,8 +227,7 @@ gs_status sort_segments_in_place(gs_ctx* ctx, int kb, uint32_t kk, bool desc, vo
   gs_status st =
       prepare_status(ctx, size_t(gs::seg_plan_large_tiles(pl)) * gs::RADIX + gs::RADIX);
   if (st == GS_OK) {
-    cudaError_t e = gs::seg_plan_run(pl, buf, buf, ctx->alt_k.ptr,
-                                     static_cast<uint64_t*>(ctx->status.ptr),
+    cudaError_t e = gs::seg_plan_run(pl, in, out, scratch, static_cast<uint64_t*>(ctx->status.ptr),
                                      &ctx->work->gen_counter, ctx->err, ctx->spin_limit,
                                      ctx->props, ctx->stream);
     if (e != cudaSuccess) st = cuda_fail(ctx, e, "segment sort launch");
@@ -285,51 +285,137 @@ gs_status sample_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, v
   for (uint32_t i = 0; i < p; ++i) off[i + 1] = off[i] + counts[i];
   if (off[p] != n) return fail(ctx, GS_ERR_CUDA, "bucket sizes do not add up to n");
   phase_mark(ctx, "Exchange data");
-  return sort_segments_in_place(ctx, kb, kk, desc, out, n, off);
+  return sort_segments(ctx, kb, kk, desc, out, out, ctx->alt_k.ptr, n, off);
 }
 
-// HykSort shape (keys only): each of p partitions sorted on its own, then
-// merged by a tree of merge-path merges. p must be a power of two (the
-// reference falls back to SampleSort otherwise,
-// include/hyksort_common_vector.inl:31-43).
+// HykSort shape (keys only), the reference's algorithm on p partitions of
+// one array (include/helpers/hyksort_helper.h:94-145 and 453-536): the
+// partitions (the ranks' data, n/p keys each) are sorted on their own, then
+// log_k(p) rounds each select k-1 splitters per group of ranks, cut every
+// rank's run at them and merge every receiving rank's k pieces in one pass
+// (hyk.cu). p and k must be powers of two, else the reference runs
+// SampleSort (include/hyksort_common_vector.inl:31-43); k larger than the
+// group is reduced to the group size (hyksort_helper.h:462).
 gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void* out,
                           uint64_t n, uint32_t flags, const gs_opts* o) {
-  uint32_t p = (o && o->partitions) ? o->partitions : 4;
+  const uint32_t p = (o && o->partitions) ? o->partitions : 4;
   const uint32_t k = (o && o->k_way) ? o->k_way : 4;
   const bool pow2 = p && !(p & (p - 1)) && k && !(k & (k - 1));
   if (!pow2) return sample_sort_device(ctx, kb, kk, in, out, n, flags, o);
+  if (p > gs::HYK_MAX_RANKS || k < 2 || k > gs::MAX_KWAY)
+    return fail(ctx, GS_ERR_INVALID, "HykSort shape: at most " + std::to_string(gs::HYK_MAX_RANKS) +
+                                         " partitions and 2 <= k_way <= " +
+                                         std::to_string(gs::MAX_KWAY));
   const bool desc = flags & GS_FLAG_DESCENDING;
   gs_status st = ensure(ctx, ctx->alt_k, size_t(n) * kb);
   if (st != GS_OK) return st;
+  uint32_t rounds = 0;
+  for (uint32_t np = p; np > 1; np /= std::min(k, np)) ++rounds;
+  // The rounds alternate between the output and the scratch buffer; the
+  // local sorts write the one that makes the last round land in `out` (in
+  // place they write `out`, and an odd round count ends with a copy).
+  const bool in_place = in == out;
+  void* alt = ctx->alt_k.ptr;
+  void* cur = (in_place || rounds % 2 == 0) ? out : alt;
+  std::vector<uint64_t> roff(p + 1);
   const uint64_t run = (n + p - 1) / p;
-  std::vector<uint64_t> off(p + 1);
-  for (uint32_t i = 0; i <= p; ++i) off[i] = std::min<uint64_t>(uint64_t(i) * run, n);
-  if (in != out) {
-    cudaError_t e = cudaMemcpyAsync(out, in, size_t(n) * kb, cudaMemcpyDeviceToDevice, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
-  }
-  st = sort_segments_in_place(ctx, kb, kk, desc, out, n, off);
+  for (uint32_t i = 0; i <= p; ++i) roff[i] = std::min<uint64_t>(uint64_t(i) * run, n);
+  st = sort_segments(ctx, kb, kk, desc, in, cur, cur == out ? alt : out, n, roff);
   if (st != GS_OK) return st;
   phase_mark(ctx, "Local sort");
-  size_t split_words = 0;  // tiles are counted per pair of full runs: any level may need the most
-  for (uint64_t r = run; r < n; r *= 2)
-    split_words = std::max(split_words, gs::merge_split_words(n, r, kb));
-  st = ensure(ctx, ctx->merge_splits, std::max<size_t>(split_words, 1) * sizeof(uint64_t));
+  if (rounds == 0) return GS_OK;
+
+  // Device scratch: rank offsets, splitters, selection rounds, cuts, pieces
+  // (fixed sizes), then the merge samples (grown per round).
+  const uint32_t kmax = std::min(k, p);
+  const size_t b_roff = size_t(p + 1) * 8, b_split = size_t(p) * gs::MAX_KWAY * 8,
+               b_iters = size_t(p) * 4, b_cuts = size_t(p) * (kmax + 1) * 8,
+               b_pieces = size_t(p) * kmax * sizeof(gs::HykPiece);
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  st = ensure(ctx, ctx->hyk_small, al(b_roff) + al(b_split) + al(b_iters) + al(b_cuts) +
+                                       al(b_pieces));
   if (st != GS_OK) return st;
-  void* cur = out;
-  void* other = ctx->alt_k.ptr;
-  for (uint64_t r = run; r < n; r *= 2) {
-    cudaError_t e = gs::launch_merge_pass(cur, other, n, r, kb, kk, desc,
-                                          static_cast<uint64_t*>(ctx->merge_splits.ptr),
-                                          ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "merge launch");
-    std::swap(cur, other);
+  uint8_t* sm = static_cast<uint8_t*>(ctx->hyk_small.ptr);
+  uint64_t* d_roff = reinterpret_cast<uint64_t*>(sm);
+  void* d_split = sm + al(b_roff);
+  uint32_t* d_iters = reinterpret_cast<uint32_t*>(sm + al(b_roff) + al(b_split));
+  uint64_t* d_cuts = reinterpret_cast<uint64_t*>(sm + al(b_roff) + al(b_split) + al(b_iters));
+  gs::HykPiece* d_pieces = reinterpret_cast<gs::HykPiece*>(sm + al(b_roff) + al(b_split) +
+                                                            al(b_iters) + al(b_cuts));
+  const uint64_t seed = o ? o->seed : 0;
+  uint32_t np = p;
+  for (uint32_t round = 0; np > 1; ++round) {
+    gs::HykRound r;
+    r.kway = std::min(k, np);
+    r.data = cur;
+    r.roff = d_roff;
+    r.p = p;
+    r.n_p = np;
+    r.key_bytes = kb;
+    r.key_kind = kk;
+    r.desc = desc;
+    r.seed = seed * 0x9E3779B97F4A7C15ull + round;
+    r.splitters = d_split;
+    r.iters = d_iters;
+    r.cuts = d_cuts;
+    if (gs::hyk_select_smem(kb, np, r.kway) > ctx->props.smem_optin)
+      return fail(ctx, GS_ERR_INVALID, "HykSort shape: splitter selection does not fit shared memory");
+    cudaError_t e = cudaMemcpyAsync(d_roff, roff.data(), b_roff, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = gs::launch_hyk_select(r, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "splitter selection launch");
+    std::vector<uint64_t> cuts(size_t(p) * (r.kway + 1));
+    e = cudaMemcpyAsync(cuts.data(), d_cuts, cuts.size() * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "splitter selection");
+    phase_mark(ctx, "Select splitters");
+    // Rank g*np + b*blk + q receives piece b of ranks g*np + i*blk + q
+    // (hyksort_helper.h:555-600: partner = blk_size * i + new_pid).
+    const uint32_t blk = np / r.kway;
+    const uint32_t stride = gs::hyk_sample_stride(kb, r.kway);
+    std::vector<gs::HykPiece> pieces(size_t(p) * r.kway);
+    std::vector<uint64_t> noff(p + 1, 0);
+    uint64_t nsamples = 0;
+    for (uint32_t rr = 0; rr < p; ++rr) {
+      const uint32_t g = rr / np, b = (rr % np) / blk, q = rr % blk;
+      uint64_t len = 0;
+      for (uint32_t i = 0; i < r.kway; ++i) {
+        const uint32_t from = g * np + i * blk + q;
+        const uint64_t* c = &cuts[size_t(from) * (r.kway + 1)];
+        gs::HykPiece& pc = pieces[size_t(rr) * r.kway + i];
+        pc.src = roff[from] + c[b];
+        pc.len = c[b + 1] - c[b];
+        pc.sample0 = nsamples;
+        pc.out = noff[rr];
+        pc.first = rr * r.kway;
+        pc.j = i;
+        nsamples += (pc.len + stride - 1) / stride;
+        len += pc.len;
+      }
+      noff[rr + 1] = noff[rr] + len;
+    }
+    if (noff[p] != n) return fail(ctx, GS_ERR_CUDA, "HykSort shape: pieces do not add up to n");
+    st = ensure(ctx, ctx->hyk_samples, size_t(std::max<uint64_t>(nsamples, 1)) * (16 + 8 * r.kway));
+    if (st != GS_OK) return st;
+    r.samp_rank = static_cast<uint64_t*>(ctx->hyk_samples.ptr);
+    r.samp_next = reinterpret_cast<int64_t*>(r.samp_rank + nsamples);
+    r.samp_cut = reinterpret_cast<uint64_t*>(r.samp_next + nsamples);
+    e = cudaMemcpyAsync(d_pieces, pieces.data(), pieces.size() * sizeof(gs::HykPiece),
+                        cudaMemcpyHostToDevice, ctx->stream);
+    void* next = cur == out ? alt : out;
+    if (e == cudaSuccess)
+      e = gs::launch_hyk_merge(r, d_pieces, uint32_t(pieces.size()), nsamples, cur, next,
+                               ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // pieces and cuts are reused
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "k-way merge");
+    phase_mark(ctx, "Merge data");
+    roff.swap(noff);
+    cur = next;
+    np = blk;
   }
   if (cur != out) {
     cudaError_t e = cudaMemcpyAsync(out, cur, size_t(n) * kb, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
   }
-  phase_mark(ctx, "Merge data");
   return GS_OK;
 }
 
@@ -509,7 +595,8 @@ void gs_ctx_destroy(gs_ctx* ctx) {
   cudaSetDevice(ctx->props.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->status, &ctx->alt_k, &ctx->alt_v, &ctx->stage_k, &ctx->stage_v,
-                    &ctx->stage_off, &ctx->splitters, &ctx->merge_splits, &ctx->third_k};
+                    &ctx->stage_off, &ctx->splitters, &ctx->hyk_small, &ctx->hyk_samples,
+                    &ctx->third_k};
   for (DevBuf* b : bufs) if (b->ptr) cudaFree(b->ptr);
   if (ctx->work) cudaFree(ctx->work);
   if (ctx->err) cudaFree(ctx->err);

@@ -104,8 +104,11 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 
 // Exclusive scan of one value per thread over the first 256 threads of the
 // block (all threads of the block must call it; threads >= 256 pass 0).
-// `s_tmp` holds at least 8 words. Returns the exclusive prefix.
-__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_tmp) {
+// `s_tmp` holds at least 8 words. Returns the exclusive prefix; with `s_out`
+// the first 256 threads also store it there, visible to the whole block on
+// return.
+__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_tmp,
+                                                        uint32_t* s_out = nullptr) {
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
@@ -121,8 +124,10 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
   if (tid < 256) {
     for (int w = 0; w < warp; ++w) wsum += s_tmp[w];
   }
+  const uint32_t ex = wsum + x - v;
+  if (s_out != nullptr && tid < 256) s_out[tid] = ex;
   __syncthreads();
-  return wsum + x - v;
+  return ex;
 }
 
 }  // namespace gs

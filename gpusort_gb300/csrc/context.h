@@ -52,7 +52,8 @@ struct gs_ctx {
   gs::DevBuf alt_k, alt_v;
   gs::DevBuf stage_k, stage_v, stage_off;
   gs::DevBuf splitters;  // sample sort
-  gs::DevBuf merge_splits;  // HykSort shape: merge-path splits of one level
+  gs::DevBuf hyk_small;     // HykSort shape: offsets, splitters, cuts, pieces
+  gs::DevBuf hyk_samples;   // HykSort shape: the merge samples of one round
   // phase timing
   cudaEvent_t ev[8] = {};
   int n_phases = 0;

@@ -85,7 +85,9 @@ int radix_num_shapes();
 // Threads per CTA and items per thread of a pass shape (false: no such shape).
 bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads, uint32_t* items);
 int radix_default_shape(int key_bytes, int val_bytes, uint64_t n);
-// Look-back words of a 32-bit keys-only job run with the default shape.
+// Tile (keys) of shape 0 for 32-bit keys without payload, and the look-back
+// words of a job run with that shape.
+constexpr uint32_t RADIX_TILE_U32_SHAPE0 = 512 * 24;
 size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
@@ -155,12 +157,42 @@ cudaError_t launch_sample_bucketing(const RadixJob& job, const SampleJob& sj,
 cudaError_t launch_bucket_pass(const RadixJob& job, const void* splitters, uint32_t nsplit,
                                const DeviceProps& props, cudaStream_t st);
 
-// One level of the merge tree: merge adjacent sorted runs of length `run`
-// of `in` (n keys, order of key_kind/desc) into runs of 2*run in `out`.
-// `splits` is device scratch of merge_split_words(n, run, key_bytes) words.
-size_t merge_split_words(uint64_t n, uint64_t run, int key_bytes);
-cudaError_t launch_merge_pass(const void* in, void* out, uint64_t n, uint64_t run, int key_bytes,
-                              uint32_t key_kind, bool desc, uint64_t* splits, cudaStream_t st);
+// HykSort shape (hyk.cu): one round of the reference's SortAmongProcesses
+// over p ranks, whose sorted runs lie at roff[r] .. roff[r+1] of `data`, in
+// groups of n_p consecutive ranks, k-way (kway <= n_p, powers of two).
+constexpr uint32_t MAX_KWAY = 16;
+constexpr uint32_t HYK_MAX_RANKS = 512;
+struct HykRound {
+  const void* data = nullptr;
+  const uint64_t* roff = nullptr;  // device, p + 1
+  uint32_t p = 0, n_p = 0, kway = 0;
+  int key_bytes = 4;
+  uint32_t key_kind = 0;
+  bool desc = false;
+  uint64_t seed = 0;
+  void* splitters = nullptr;       // device, (p / n_p) x (kway - 1) keys
+  uint32_t* iters = nullptr;       // device, p / n_p (selection rounds, diagnostic)
+  uint64_t* cuts = nullptr;        // device, p x (kway + 1) cut offsets
+  uint64_t* samp_rank = nullptr;   // device, per merge sample
+  uint64_t* samp_cut = nullptr;    // device, per merge sample x kway
+  int64_t* samp_next = nullptr;    // device, per merge sample
+};
+// One of the kway pieces a receiving rank merges: src .. src + len of the
+// source buffer; the rank's output starts at `out`; its pieces are
+// first .. first + kway - 1 of the table; the piece's merge samples (one
+// every hyk_sample_stride elements) are numbered from sample0.
+struct HykPiece {
+  uint64_t src, len, sample0, out;
+  uint32_t first, j;
+};
+uint32_t hyk_sample_stride(int key_bytes, uint32_t kway);
+size_t hyk_select_smem(int key_bytes, uint32_t n_p, uint32_t kway);
+// Splitter selection (one CTA per group) and the ranks' cut points.
+cudaError_t launch_hyk_select(const HykRound& r, cudaStream_t st);
+// The k-way merge of every receiving rank's pieces from src into dst.
+cudaError_t launch_hyk_merge(const HykRound& r, const HykPiece* pieces, uint32_t npieces,
+                             uint64_t nsamples, const void* src, void* dst, cudaStream_t st);
+
 
 // Allow `kern` up to `bytes` of dynamic shared memory on the current device
 // (once per kernel and device; safe to call from any thread).

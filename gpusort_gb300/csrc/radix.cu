@@ -77,63 +77,52 @@ constexpr uint32_t UPSWEEP_SMEM = 64u << 10;  // column-spread histograms per CT
 constexpr int UPSWEEP_PER_SM = 3;
 
 // Tile shapes of the pass kernel (threads per block, items per thread,
-// blocks per SM), selectable per call; shape 0 is the default. Larger
-// elements take fewer items per thread.
-template <int T, int I, int B, int C = 8> struct Shape {
-  static constexpr int THREADS = T, ITEMS = I, MINB = B, CLUSTER = C;
+// blocks per SM, ranking of the stable passes), selectable per call; shape
+// 0 is the default. Larger elements take fewer items per thread. Shapes 0
+// and 2 share a geometry and differ in the ranking: half-warp ranking is
+// faster for keys (2^30 u32: 16.0 vs 16.8 ms; 2^29 u64: 24.7 vs 25.7 ms),
+// the 64-bit table for key/value pairs (2^29 u64 + u32: 56.0 vs 56.6 ms).
+template <int T, int I, int B, int R = RANK_TABLE> struct Shape {
+  static constexpr int THREADS = T, ITEMS = I, MINB = B, RANK = R;
 };
 template <typename K, typename V, int S> struct PassShape;
-// Shape 2 of keys-only sorts uses thread-block clusters (one look-back per
-// 8 tiles); it measured slower than per-tile look-back on GB300 and is kept
-// selectable for tuning. Key/value sorts never use clusters: a clustered
-// 256-thread pair variant raised an illegal-instruction fault on GB300
-// whose cause is not yet understood.
-template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 24, 2, 1> {};
-template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 20, 4, 1> {};
-template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 16, 2, 8> {};
-template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 14, 2, 1> {};
-template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4, 1> {};
-template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 12, 2, 8> {};
-template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 14, 2, 1> {};
-template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4, 1> {};
-template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<256, 10, 4, 1> {};
+template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 24, 2, RANK_HALF> {};
+template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 20, 4> {};
+template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 24, 2> {};
+template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 14, 2, RANK_HALF> {};
+template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4> {};
+template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 14, 2> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 14, 2> {};
+template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4> {};
+template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<512, 14, 2, RANK_HALF> {};
+template <> struct PassShape<uint64_t, uint64_t, 0> : Shape<512, 9, 2> {};
+template <> struct PassShape<uint64_t, uint64_t, 2> : Shape<512, 9, 2, RANK_HALF> {};
 template <typename K, typename V, int S>
-struct PassShape : Shape<(S == 0 ? 512 : 256), (S == 0 ? 10 : 6), (S == 0 ? 2 : 4), 1> {};
+struct PassShape : Shape<(S == 1 ? 256 : 512), (S == 1 ? 6 : 10), (S == 1 ? 4 : 2),
+                         (S == 2 ? RANK_HALF : RANK_TABLE)> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 1024;  // no shape has a smaller tile (smallest: 256 x 6)
 
 // Enqueue the digit passes (plan already in job.work). With `sj` the passes
-// sort the large segments of a batch; the shape must then run without
-// clusters.
+// sort the large segments of a batch.
 template <typename K, typename V, int S>
 cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits, uint32_t vd,
                           const DeviceProps& props, uint32_t* gen, cudaStream_t stream) {
-  constexpr int PASS_THREADS = PassShape<K, V, S>::THREADS;
-  constexpr int ITEMS = PassShape<K, V, S>::ITEMS;
-  constexpr int MINB = PassShape<K, V, S>::MINB;
-  constexpr int CLUSTER = PassShape<K, V, S>::CLUSTER;
-  using Cfg = PassConfig<K, V, PASS_THREADS, ITEMS>;
+  using Sh = PassShape<K, V, S>;
+  using Cfg = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, Sh::RANK>;
+  // The lowest digit's pass, when it runs, is the first one and ranks
+  // unstably (keys only): half-warp ranking gains nothing there and its
+  // larger offset table costs L1 capacity (2^30 u32: 3.05 vs 3.20 ms), so
+  // that launch takes the table variant of the same tile.
+  using Cfg0 = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, RANK_TABLE>;
+  static_assert(Cfg0::TILE == Cfg::TILE, "one tile layout for every pass of a sort");
   cudaError_t e = cudaSuccess;
-  auto kern = pass_kernel<K, V, PASS_THREADS, ITEMS, MINB, CLUSTER>;
+  auto kern = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK>;
+  auto kern0 = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, RANK_TABLE>;
   e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
+  if (e == cudaSuccess) e = allow_dynamic_smem(reinterpret_cast<const void*>(kern0), Cfg0::DYN_SMEM);
   if (e != cudaSuccess) return e;
-  if (sj != nullptr && CLUSTER > 1) return cudaErrorInvalidValue;
   const uint64_t tiles = sj != nullptr ? sj->total_tiles : (job.n + Cfg::TILE - 1) / Cfg::TILE;
-  const uint64_t units = (tiles + CLUSTER - 1) / CLUSTER;  // look-back units (cluster-tiles)
-  cudaLaunchConfig_t lc = {};
-  cudaLaunchAttribute attr[1];
-  lc.gridDim = dim3(unsigned(units * CLUSTER));
-  lc.blockDim = dim3(PASS_THREADS);
-  lc.dynamicSmemBytes = Cfg::DYN_SMEM;
-  lc.stream = stream;
-  if (CLUSTER > 1) {
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CLUSTER;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    lc.attrs = attr;
-    lc.numAttrs = 1;
-  }
   PassParams pa{};
   pa.keys_in = job.keys_in;
   pa.keys_out = job.keys_out;
@@ -164,9 +153,14 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   (void)gen;
   const uint32_t qlo = job.digit_hi ? job.digit_lo : 0u;
   const uint32_t qhi = job.digit_hi ? job.digit_hi : digits;
+  const bool table_first = Sh::RANK == RANK_HALF && pa.first_unstable;
   for (uint32_t q = qlo; q < qhi; ++q) {
     pa.pass = q;
-    e = cudaLaunchKernelEx(&lc, kern, pa);
+    if (q == qlo && table_first)
+      kern0<<<unsigned(tiles), Sh::THREADS, Cfg0::DYN_SMEM, stream>>>(pa);
+    else
+      kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM, stream>>>(pa);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (job.marks) cudaEventRecord(job.marks[3 + q], stream);
   }
@@ -308,7 +302,7 @@ uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape) {
 }
 
 int radix_segmented_shape(int key_bytes, uint64_t n, uint32_t nseg) {
-  // Non-cluster shapes only. Many moderate segments: the 256-thread shape
+  // Many moderate segments: the 256-thread shape
   // (100,000 segments of 16 .. 2^22 keys, ~2^30 in all: 23.0 ms vs 23.8 ms
   // with 512 x 24 tiles, which leave more of each segment's last tile
   // empty). Few large segments (the SampleSort and HykSort shapes' buckets
@@ -337,9 +331,10 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
 template <typename K>
 cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t nsplit,
                           const DeviceProps& props, cudaStream_t st) {
-  // 16 items per thread leave registers for the packed bucket ids.
-  using Sh = Shape<512, 16, 2, 1>;
-  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS>;
+  // 16 (32-bit keys) or 12 (64-bit keys) items per thread leave registers
+  // for the packed bucket ids.
+  using Sh = Shape<512, sizeof(K) == 4 ? 16 : 12, 2>;
+  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::RANK>;
   PlanParams pp{};
   pp.work = job.work;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
@@ -349,7 +344,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.digit_lo = 0;
   pp.digit_hi = 1;
   plan_kernel<<<1, 256, 0, st>>>(pp);
-  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, 1, true>;
+  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK, true>;
   cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM_BUCKET);
   if (e != cudaSuccess) return e;
   PassParams pa{};
@@ -430,10 +425,9 @@ bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads
 // shape is fastest for every key and value width; its items per thread are
 // the most that fit 64 registers without spilling (u32 keys 512 x 24: 2^29
 // in 9.40 ms vs 10.71 at 16 items; u64 keys 512 x 14: 26.99 vs 28.57 ms at
-// 12; u64 + u32 pairs 512 x 10: 37.7 vs 41.7 ms at 8). The clustered shape
-// is slowest everywhere. Up to 2^18 keys (no payload) a sort is a few tiles
-// per pass and each pass takes about one tile's latency, so the smaller
-// 256-thread tiles win: 2^16 u32 keys 52.9 vs 65.0 us, u64 86.2 vs 102.7 us;
+// 12; u64 + u32 pairs 512 x 10: 37.7 vs 41.7 ms at 8). Up to 2^18 keys
+// (no payload) a sort is a few tiles per pass and each pass takes about one
+// tile's latency, so the smaller 256-thread tiles win: 2^16 u32 keys 52.9 vs 65.0 us, u64 86.2 vs 102.7 us;
 // equal or worse from 2^20.
 int radix_default_shape(int key_bytes, int val_bytes, uint64_t n) {
   (void)key_bytes;
@@ -448,6 +442,7 @@ size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes) {
 size_t radix_status_words_u32_shape0(uint64_t n) {
   constexpr uint64_t t = uint64_t(PassShape<uint32_t, NoValue, 0>::THREADS) *
                          PassShape<uint32_t, NoValue, 0>::ITEMS;
+  static_assert(t == RADIX_TILE_U32_SHAPE0, "engine.h states the shape-0 tile");
   return size_t((n + t - 1) / t) * RADIX;
 }
 

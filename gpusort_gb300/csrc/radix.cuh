@@ -20,8 +20,6 @@
 // pipeline is graph-capturable.
 #pragma once
 
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 #include "radix_types.cuh"
 
@@ -189,7 +187,25 @@ upsweep_kernel(UpsweepParams p) {
 // ---------------------------------------------------------------------------
 // One onesweep pass.
 // ---------------------------------------------------------------------------
-template <typename K, typename V, int THREADS, int ITEMS>
+// Ranking of the stable passes (a pass-kernel template parameter):
+//   RANK_TABLE - each lane sets its bit in the digit's peer mask in a
+//                per-warp shared table, reads the mask back with the digit's
+//                running count (one 64-bit word), and the group's lowest
+//                lane advances the count: three shared accesses per element;
+//   RANK_HALF  - the same with each 16-lane half of a warp ranking on its
+//                own, so that a digit's peer mask (16 bits) and running
+//                count (16 bits) share one 32-bit word: the accesses spread
+//                over all 32 banks, where the 64-bit entries of RANK_TABLE
+//                use 16 bank pairs. A half-warp's items are a contiguous run
+//                of the input, so ranking half 0 before half 1 keeps input
+//                order. Measured on GB300 (2^30 u32 keys): stable passes
+//                3.97 ms vs 4.30 ms; shared-memory bank conflicts are what
+//                bound the pass. Eight warp ballots per row instead of the
+//                peer table halve the shared-memory wavefronts but triple
+//                the ALU instructions and made the pass ALU-bound (4.51 ms).
+enum RankMode : int { RANK_TABLE = 0, RANK_HALF = 2 };
+
+template <typename K, typename V, int THREADS, int ITEMS, int RANK = RANK_TABLE>
 struct PassConfig {
   static constexpr int WARPS = THREADS / 32;
   static constexpr int TILE = THREADS * ITEMS;
@@ -198,14 +214,24 @@ struct PassConfig {
   static constexpr size_t VAL_BYTES = HAS_V ? sizeof(typename std::conditional<HAS_V, V, uint32_t>::type) : 0;
   static constexpr size_t SMEM_KEYS = size_t(TILE) * sizeof(K);
   static constexpr size_t SMEM_VALS = size_t(TILE) * VAL_BYTES;
-  // Dynamic shared memory: the ranking table (per warp and digit, 64-bit)
-  // and the reorder staging of the tile are never live at the same time,
-  // so they share one region; the per-warp digit offsets, live from the
-  // count phase to the end of the reorder, follow it.
-  static constexpr size_t TAB_BYTES = size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t);
+  // Dynamic shared memory: the ranking table (per warp and digit: a 64-bit
+  // mask and count for RANK_TABLE, two 32-bit ones for RANK_HALF) and the
+  // reorder staging of the tile are never live at the same time, so they
+  // share one region; the per-ranker digit offsets, live from the count
+  // phase to the end of the reorder, follow it.
+  // Items of one ranker (a warp, or a half-warp for RANK_HALF) are STRIDE
+  // apart in the tile.
+  static constexpr int STRIDE = RANK == RANK_HALF ? 16 : 32;
+  static constexpr size_t TAB_BYTES =
+      RANK == RANK_TABLE ? size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t)
+                         : ((size_t(WARPS) * (RADIX + 1) * 2 * sizeof(uint32_t) + 15) & ~size_t(15));
+  static_assert(TAB_BYTES % 16 == 0, "the table is cleared in 16-byte units");
   static constexpr size_t STAGE_BYTES = SMEM_KEYS + SMEM_VALS;
   static constexpr size_t UNION_BYTES = ((STAGE_BYTES > TAB_BYTES ? STAGE_BYTES : TAB_BYTES) + 15) & ~size_t(15);
-  static constexpr size_t OFF_BYTES = size_t(WARPS) * RADIX * sizeof(uint16_t);
+  // Per warp and digit: a 16-bit tile offset, or (RANK_HALF) two, one per
+  // half, in one 32-bit word.
+  using OffT = typename std::conditional<RANK == RANK_HALF, uint32_t, uint16_t>::type;
+  static constexpr size_t OFF_BYTES = size_t(WARPS) * RADIX * sizeof(OffT);
   static constexpr size_t DYN_SMEM = UNION_BYTES + OFF_BYTES;
   // BUCKET mode also stages each element's bucket (one byte) for the scatter.
   static constexpr size_t DYN_SMEM_BUCKET = DYN_SMEM + size_t(TILE);
@@ -248,38 +274,18 @@ __device__ __forceinline__ uint32_t tree_bucket(const K* tree, uint32_t levels, 
   return b < nsplit ? b : nsplit;  // padding slots equal to y == ~0 count past the end
 }
 
-
 // Keys live in the transformed domain between passes: the first pass that
 // runs transforms them on load, the last one restores raw bits on store.
 // Values stay raw and are transformed only to extract a value digit.
-// With CLUSTER > 1, a thread-block cluster of CLUSTER CTAs takes CLUSTER
-// consecutive tiles: the CTAs combine their digit counts through
-// distributed shared memory and only the cluster's first CTA runs the
-// decoupled look-back, over cluster-tiles. Look-back steps per pass drop
-// by CLUSTER, which is what bounds the pass on GB300 (the chain moves a
-// few tiles per L2 round trip).
-// Cluster barrier halves. The warp is reconverged first and the non-.aligned
-// forms are used, because the calls follow divergent code (partial tiles).
-__device__ __forceinline__ void cluster_arrive() {
-  __syncwarp();
-  asm volatile("barrier.cluster.arrive.release;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_wait() {
-  __syncwarp();
-  asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
-}
-__device__ __forceinline__ void cluster_sync() {
-  cluster_arrive();
-  cluster_wait();
-}
-
-template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int CLUSTER,
+template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int RANK = RANK_TABLE,
           bool BUCKET = false>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 pass_kernel(PassParams p) {
-  using Cfg = PassConfig<K, V, THREADS, ITEMS>;
+  using Cfg = PassConfig<K, V, THREADS, ITEMS, RANK>;
   constexpr int WARPS = Cfg::WARPS;
   constexpr int TILE = Cfg::TILE;
+  constexpr int STRIDE = Cfg::STRIDE;
+  using OffT = typename Cfg::OffT;
   constexpr bool HAS_V = Cfg::HAS_V;
   constexpr int LB_WIN = 4;         // look-back words read per round
   constexpr int LB_SLEEP_NS = 128;  // pause after a round without progress
@@ -287,31 +293,31 @@ pass_kernel(PassParams p) {
 
   extern __shared__ __align__(16) uint8_t s_dyn[];
   // Ranking table, in the region the reorder stages the tile in later.
-  // Stable ranking: per warp and digit, the peer mask of the current item
-  // row and the running count (mask in the low half for even digits, in the
-  // high half for odd ones). The unstable ranking uses its first RADIX
+  // RANK_TABLE: per warp and digit, the peer mask of the current item row
+  // and the running count (mask in the low half for even digits, in the
+  // high half for odd ones). The unstable ranking uses the first RADIX
   // 32-bit words as tile counters.
   uint64_t (*const s_tab)[RADIX + 1] = reinterpret_cast<uint64_t (*)[RADIX + 1]>(s_dyn);
-  // Per warp and digit: the warp's start of the digit in the tile (stable
-  // ranking); row 0 holds the tile offsets of the unstable ranking. 16-bit
+  // RANK_HALF: per warp, digit and half: peer mask (low 16 bits) and
+  // running count (high 16 bits).
+  uint32_t (*const s_htab)[RADIX + 1][2] = reinterpret_cast<uint32_t (*)[RADIX + 1][2]>(s_dyn);
+  // Per warp and digit: the ranker's start of the digit in the tile (stable
+  // ranking; RANK_HALF: half 0 in the low 16 bits, half 1 in the high 16);
+  // row 0 holds the tile offsets of the unstable ranking. 16-bit fields
   // (offsets are below the tile size, at most 65536): less shared memory
   // per CTA measured faster (2^30 u32 keys: 17.30 vs 17.61 ms).
-  uint16_t (*const s_offd)[RADIX] = reinterpret_cast<uint16_t (*)[RADIX]>(s_dyn + Cfg::UNION_BYTES);
+  OffT (*const s_offd)[RADIX] = reinterpret_cast<OffT (*)[RADIX]>(s_dyn + Cfg::UNION_BYTES);
   __shared__ uint32_t s_dst_base[RADIX];
+  __shared__ uint32_t s_excl[RADIX];  // the tile's exclusive digit offsets
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_seg;
   __shared__ uint32_t s_bad;  // a digit's destination range leaves the output
   __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode: splitter search tree
-  __shared__ uint32_t s_pub[CLUSTER > 1 ? RADIX : 1];     // this CTA's digit counts
-  __shared__ uint32_t s_prefix[CLUSTER > 1 ? RADIX : 1];  // cluster-tile prefix (rank 0)
 
   SortPlan& plan = p.work->plan;
   const uint32_t j = plan.exec_index[p.pass];
   if (j == PASS_SKIPPED) return;
-  namespace cg = cooperative_groups;
-  uint32_t crank = 0;
-  if constexpr (CLUSTER > 1) crank = cg::this_cluster().block_rank();
   const uint32_t m = plan.m_exec;
   const uint32_t gen = (plan.gen_base + p.pass + 1) & GEN_MASK;  // this pass's look-back tag
   const bool first = (j == 0);
@@ -348,30 +354,25 @@ pass_kernel(PassParams p) {
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const OrderXform<VS> vx(p.val_kind, p.desc != 0);
 
-  // Tiles (cluster-tiles) are claimed in launch order, so a tile only ever
-  // waits on tiles held by CTAs that are already running.
-  if (tid == 0 && crank == 0) s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
-  if (tid == 0) s_bad = 0;
-  if ((smem_addr(&s_tab[0][0]) & 15u) == 0) {
-    static_assert((WARPS * (RADIX + 1)) % 2 == 0, "s_tab is cleared in 16-byte units");
-    uint4* z = reinterpret_cast<uint4*>(&s_tab[0][0]);
-    constexpr int Z = WARPS * (RADIX + 1) / 2;
+  // Tiles are claimed in launch order, so a tile only ever waits on tiles
+  // held by CTAs that are already running.
+  if (tid == 0) {
+    s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
+    s_bad = 0;
+  }
+  if ((smem_addr(s_dyn) & 15u) == 0) {
+    uint4* z = reinterpret_cast<uint4*>(s_dyn);
+    constexpr int Z = int(Cfg::TAB_BYTES / 16);
     for (int i = tid; i < Z; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
-  } else {  // not expected (the table is declared 16-byte aligned)
-    for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&s_tab[0][0])[i] = 0ull;
+  } else {  // not expected (the region is declared 16-byte aligned)
+    uint32_t* z = reinterpret_cast<uint32_t*>(s_dyn);
+    for (int i = tid; i < int(Cfg::TAB_BYTES / 4); i += THREADS) z[i] = 0u;
     if (tid == 0) atomicOr(p.err, ERR_SMEM_ALIGN);
   }
-  uint32_t ctile;  // unit of the look-back: a tile, or a cluster-tile
-  if constexpr (CLUSTER > 1) {
-    cluster_sync();
-    ctile = *cg::this_cluster().map_shared_rank(&s_tile, 0);
-  } else {
-    __syncthreads();
-    ctile = s_tile;
-  }
-  const uint32_t tile = ctile * CLUSTER + crank;
-  // Batched sorts (CLUSTER == 1): the tile's segment, its element range and
-  // its first tile, where the segment's look-back chain starts.
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  // Batched sorts: the tile's segment, its element range and its first
+  // tile, where the segment's look-back chain starts.
   uint32_t seg = 0, first_unit = 0;
   uint64_t e0 = 0, e1 = n;
   if (p.seg_tile_start != nullptr) {
@@ -392,7 +393,10 @@ pass_kernel(PassParams p) {
   const uint64_t tile_base = e0 + uint64_t(tile - first_unit) * TILE;
   const uint32_t tile_n =
       tile_base >= e1 ? 0u : uint32_t(e1 - tile_base < uint64_t(TILE) ? e1 - tile_base : uint64_t(TILE));
-  const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;  // tile index of item 0
+  // Tile index of item 0; item i is STRIDE further. RANK_HALF: lanes 0-15
+  // and 16-31 of a warp hold two consecutive runs of 16 * ITEMS elements.
+  const uint32_t ranker = RANK == RANK_HALF ? uint32_t(2 * warp + (lane >> 4)) : uint32_t(warp);
+  const uint32_t wloc = ranker * STRIDE * ITEMS + uint32_t(lane & (STRIDE - 1));
   const uint32_t nsplit = p.nsplit;
   const uint32_t split_levels = BUCKET ? tree_levels(nsplit) : 0u;
   if constexpr (BUCKET) {
@@ -415,255 +419,294 @@ pass_kernel(PassParams p) {
     return tree_bucket(s_split, split_levels, nsplit, y);
   };
 
-  // Load: item i of lane l is tile element wloc + 32*i, so (i, lane) order
-  // is input order and the stable ranking below keeps it.
-  K keys[ITEMS];
-  VS vals[HAS_V ? ITEMS : 1];
-  if (!reverse) {
-    const K* sk = src_k + tile_base + wloc;
-    const VS* sv = nullptr;
-    if constexpr (HAS_V) sv = src_v + tile_base + wloc;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const bool valid = wloc + 32 * i < tile_n;
-      keys[i] = valid ? ld_stream(sk + 32 * i) : K(0);
-      if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv + 32 * i) : VS(0);
-    }
-  } else {
-    const K* sk = src_k + (n - 1 - tile_base - wloc);
-    const VS* sv = nullptr;
-    if constexpr (HAS_V) sv = src_v + (n - 1 - tile_base - wloc);
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const bool valid = wloc + 32 * i < tile_n;
-      keys[i] = valid ? ld_stream(sk - 32 * i) : K(0);
-      if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv - 32 * i) : VS(0);
-    }
-  }
-  if (first) {
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) keys[i] = kx.fwd(keys[i]);
-  }
-  // BUCKET mode: each item's bucket is searched once and kept, one byte each.
-  uint32_t bdig[BUCKET ? (ITEMS + 3) / 4 : 1];
-  if constexpr (BUCKET) {
-#pragma unroll
-    for (int i = 0; i < (ITEMS + 3) / 4; ++i) bdig[i] = 0;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
-      if (wloc + 32 * i < tile_n) bdig[i >> 2] |= key_digit(keys[i]) << (8 * (i & 3));
-  }
-  auto digit_at = [&](int i) -> uint32_t {
-    if constexpr (BUCKET) return (bdig[i >> 2] >> (8 * (i & 3))) & 0xFFu;
-    if constexpr (HAS_V) {
-      if (from_val) return uint32_t(vx.fwd(vals[i]) >> shift) & (RADIX - 1);
-    }
-    return key_digit(keys[i]);
-  };
+  // The tile's work; FULL tiles (all but a pass's last, and a segment's
+  // last) need no per-element bounds checks.
+  auto body = [&](auto full_c) {
+    constexpr bool FULL = decltype(full_c)::value;
+    auto in_tile = [&](uint32_t idx) -> bool { return FULL || idx < tile_n; };
 
-  // Ranks are below the tile size (< 2^16): two per register.
-  uint32_t rank2[(ITEMS + 1) / 2];
+    // Load: item i of lane l is tile element wloc + STRIDE*i, so (ranker,
+    // i, lane) order is input order and the stable ranking below keeps it.
+    K keys[ITEMS];
+    VS vals[HAS_V ? ITEMS : 1];
+    if (!reverse) {
+      const K* sk = src_k + tile_base + wloc;
+      const VS* sv = nullptr;
+      if constexpr (HAS_V) sv = src_v + tile_base + wloc;
 #pragma unroll
-  for (int i = 0; i < (ITEMS + 1) / 2; ++i) rank2[i] = 0;
-  auto set_rank = [&](int i, uint32_t r) { rank2[i >> 1] |= r << (16 * (i & 1)); };
-  auto get_rank = [&](int i) -> uint32_t { return (rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu; };
-
-  uint32_t* s_cnt = reinterpret_cast<uint32_t*>(&s_tab[0][0]);
-  if (unstable) {
-    // One shared atomic per element: its rank among the tile's elements of
-    // the same digit, in no particular order.
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      if (wloc + 32 * i < tile_n) set_rank(i, atomicAdd(&s_cnt[digit_at(i)], 1u));
-    }
-  } else {
-    // Stable warp ranking: each lane sets its bit in the digit's peer mask,
-    // reads back the mask and the digit's running count; the group's lowest
-    // lane advances the count and clears the mask.
-    // Odd digits keep the mask in the high half and the count in the low
-    // half, so the lanes' atomics spread over all 32 banks.
-    const uint32_t lt = lanemask_lt();
-    const uint32_t bit = 1u << lane;
-    uint64_t* tab = s_tab[warp];
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const uint32_t d = (wloc + 32 * i < tile_n) ? digit_at(i) : uint32_t(RADIX);
-      const uint32_t odd = d & 1u;
-      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]) + odd, bit);
-      __syncwarp();
-      const uint64_t e = tab[d];
-      __syncwarp();
-      const uint32_t lo = uint32_t(e), hi = uint32_t(e >> 32);
-      const uint32_t peers = odd ? hi : lo;
-      const uint32_t base = odd ? lo : hi;
-      const uint32_t below = peers & lt;
-      set_rank(i, base + __popc(below));
-      if (below == 0) {
-        const uint64_t c = base + __popc(peers);
-        tab[d] = odd ? c : (c << 32);
+      for (int i = 0; i < ITEMS; ++i) {
+        const bool valid = in_tile(wloc + STRIDE * i);
+        keys[i] = valid ? ld_stream(sk + STRIDE * i) : K(0);
+        if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv + STRIDE * i) : VS(0);
       }
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-
-  // Per digit: tile count, per-warp exclusive offsets (stable).
-  uint32_t count = 0;
-  if (tid < RADIX) {
-    if (unstable) {
-      count = s_cnt[tid];
     } else {
-      uint32_t run = 0;
+      const K* sk = src_k + (n - 1 - tile_base - wloc);
+      const VS* sv = nullptr;
+      if constexpr (HAS_V) sv = src_v + (n - 1 - tile_base - wloc);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const bool valid = in_tile(wloc + STRIDE * i);
+        keys[i] = valid ? ld_stream(sk - STRIDE * i) : K(0);
+        if constexpr (HAS_V) vals[i] = valid ? ld_stream(sv - STRIDE * i) : VS(0);
+      }
+    }
+    if (first) {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) keys[i] = kx.fwd(keys[i]);
+    }
+    // BUCKET mode: each item's bucket is searched once and kept, one byte each.
+    uint32_t bdig[BUCKET ? (ITEMS + 3) / 4 : 1];
+    if constexpr (BUCKET) {
+#pragma unroll
+      for (int i = 0; i < (ITEMS + 3) / 4; ++i) bdig[i] = 0;
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+        if (in_tile(wloc + STRIDE * i)) bdig[i >> 2] |= key_digit(keys[i]) << (8 * (i & 3));
+    }
+    auto digit_at = [&](int i) -> uint32_t {
+      if constexpr (BUCKET) return (bdig[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+      if constexpr (HAS_V) {
+        if (from_val) return uint32_t(vx.fwd(vals[i]) >> shift) & (RADIX - 1);
+      }
+      return key_digit(keys[i]);
+    };
+
+    // Ranks are below the tile size (< 2^16): two per register.
+    uint32_t rank2[(ITEMS + 1) / 2];
+#pragma unroll
+    for (int i = 0; i < (ITEMS + 1) / 2; ++i) rank2[i] = 0;
+    auto set_rank = [&](int i, uint32_t r) { rank2[i >> 1] |= r << (16 * (i & 1)); };
+    auto get_rank = [&](int i) -> uint32_t { return (rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu; };
+
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_dyn);
+    if (unstable) {
+      // One shared atomic per element: its rank among the tile's elements of
+      // the same digit, in no particular order.
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (in_tile(wloc + STRIDE * i)) set_rank(i, atomicAdd(&s_cnt[digit_at(i)], 1u));
+      }
+    } else if constexpr (RANK == RANK_HALF) {
+      // Stable half-warp ranking: as below, with a 32-bit word per digit and
+      // half (16-bit peer mask, 16-bit count); a half-warp's count of one
+      // digit is at most 16 * ITEMS.
+      static_assert(16 * ITEMS < 65536, "half-warp counts are 16-bit");
+      const uint32_t h = uint32_t(lane) >> 4;
+      const uint32_t sl = uint32_t(lane) & 15u;
+      const uint32_t lt = (1u << sl) - 1u;
+      const uint32_t bit = 1u << sl;
+      uint32_t (*tab)[2] = s_htab[warp];
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t d = in_tile(wloc + STRIDE * i) ? digit_at(i) : uint32_t(RADIX);
+        uint32_t* e = &tab[d][h];
+        atomicOr(e, bit);
+        __syncwarp();
+        const uint32_t w = *e;
+        __syncwarp();
+        const uint32_t peers = w & 0xFFFFu;
+        const uint32_t base = w >> 16;
+        const uint32_t below = peers & lt;
+        set_rank(i, base + __popc(below));
+        if (below == 0) *e = (base + __popc(peers)) << 16;
+        __syncwarp();
+      }
+    } else {
+      // Stable warp ranking: each lane sets its bit in the digit's peer mask,
+      // reads back the mask and the digit's running count; the group's lowest
+      // lane advances the count and clears the mask.
+      // Odd digits keep the mask in the high half and the count in the low
+      // half.
+      const uint32_t lt = lanemask_lt();
+      const uint32_t bit = 1u << lane;
+      uint64_t* tab = s_tab[warp];
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t d = in_tile(wloc + STRIDE * i) ? digit_at(i) : uint32_t(RADIX);
+        const uint32_t odd = d & 1u;
+        atomicOr(reinterpret_cast<uint32_t*>(&tab[d]) + odd, bit);
+        __syncwarp();
+        const uint64_t e = tab[d];
+        __syncwarp();
+        const uint32_t lo = uint32_t(e), hi = uint32_t(e >> 32);
+        const uint32_t peers = odd ? hi : lo;
+        const uint32_t base = odd ? lo : hi;
+        const uint32_t below = peers & lt;
+        set_rank(i, base + __popc(below));
+        if (below == 0) {
+          const uint64_t c = base + __popc(peers);
+          tab[d] = odd ? c : (c << 32);
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+
+    // Counts of digit d of warp w's rankers (one 64-bit word either way).
+    auto ranker_counts = [&](int w, uint32_t d, uint32_t& c0, uint32_t& c1) {
+      if constexpr (RANK == RANK_HALF) {
+        const uint2 e = *reinterpret_cast<const uint2*>(&s_htab[w][d][0]);
+        c0 = e.x >> 16;
+        c1 = e.y >> 16;
+      } else {
+        const uint64_t e = s_tab[w][d];
+        c0 = (d & 1u) ? uint32_t(e) : uint32_t(e >> 32);
+        c1 = 0;
+      }
+    };
+    // Per digit: the tile's count.
+    uint32_t count = 0;
+    if (tid < RADIX) {
+      if (unstable) {
+        count = s_cnt[tid];
+      } else {
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) {
+          uint32_t c0, c1;
+          ranker_counts(w, tid, c0, c1);
+          count += c0 + c1;
+        }
+      }
+    }
+    uint64_t* status = p.status + uint64_t(tile) * RADIX;
+    if (tid < RADIX) {
+      st_relaxed(status + tid,
+                 make_status(tile == first_unit ? FLAG_INC : FLAG_AGG, gen, count));
+    }
+    const uint32_t tile_excl = block_excl_scan_256(count, s_tmp, s_excl);
+
+    // Per warp and digit: where the ranker's elements of the digit start in
+    // the reordered tile. With 512 or more threads the upper ones write
+    // these while the first 256 run the look-back below.
+    auto write_offsets = [&](uint32_t d) {
+      uint32_t run = s_excl[d];
+      if (unstable) {
+        s_offd[0][d] = OffT(RANK == RANK_HALF ? (run | (run << 16)) : run);
+        return;
+      }
 #pragma unroll
       for (int w = 0; w < WARPS; ++w) {
-        const uint64_t e = s_tab[w][tid];
-        const uint32_t c = (tid & 1) ? uint32_t(e) : uint32_t(e >> 32);
-        s_offd[w][tid] = uint16_t(run);  // this thread owns column tid
-        run += c;
+        uint32_t c0, c1;
+        ranker_counts(w, d, c0, c1);
+        s_offd[w][d] = OffT(RANK == RANK_HALF ? (run | ((run + c0) << 16)) : run);
+        run += c0 + c1;
       }
-      count = run;
-    }
-    if constexpr (CLUSTER > 1) s_pub[tid] = count;
-  }
-  uint32_t unit_count = count;  // count of the look-back unit
-  uint32_t cl_excl = 0;         // this CTA's offset within the cluster-tile
-  const bool leader = (crank == 0);
-  if constexpr (CLUSTER > 1) {
-    cluster_sync();
-    if (tid < RADIX) {
-      uint32_t total = 0;
-#pragma unroll
-      for (int r = 0; r < CLUSTER; ++r) {
-        const uint32_t c = cg::this_cluster().map_shared_rank(s_pub, r)[tid];
-        if (r < int(crank)) cl_excl += c;
-        total += c;
-      }
-      unit_count = total;
-    }
-  }
-  uint64_t* status = p.status + uint64_t(ctile) * RADIX;
-  if (tid < RADIX && leader) {
-    st_relaxed(status + tid,
-               make_status(ctile == first_unit ? FLAG_INC : FLAG_AGG, gen, unit_count));
-  }
-  const uint32_t tile_excl = block_excl_scan_256(count, s_tmp);
-
-  // Decoupled look-back over preceding units, LB_WIN words per round,
-  // bounded by spin_limit rounds without progress (the cluster's first CTA).
-  // While the nearest word is pending, one word is polled per round after a
-  // short sleep, so waiting warps leave issue slots and L1 bandwidth to the
-  // tiles they wait for.
-  uint32_t prefix = 0;
-  if (tid < RADIX && leader) {
-    if (ctile > first_unit) {
-      int64_t t = int64_t(ctile) - 1;
-      uint32_t idle_rounds = 0;
-      const bool stall = p.inject_stall && ctile == 1;
-      int win = LB_WIN;
-      while (true) {
-        uint64_t w[LB_WIN];
-#pragma unroll
-        for (int k = 0; k < LB_WIN; ++k) {
-          const int64_t tt = t - k;
-          w[k] = (k < win && tt >= 0 && !stall) ? ld_relaxed(p.status + uint64_t(tt) * RADIX + tid)
-                                                : 0ull;
-        }
-        int consumed = 0;
-        bool done = false;
-#pragma unroll
-        for (int k = 0; k < LB_WIN; ++k) {
-          const uint64_t wk = w[k];
-          const bool ready = (wk & FLAG_MASK) != 0 && uint32_t((wk >> 32) & GEN_MASK) == gen;
-          if (!done && consumed == k && ready) {
-            prefix += uint32_t(wk);
-            consumed = k + 1;
-            done = (wk & FLAG_MASK) == FLAG_INC;
-          }
-        }
-        if (done) break;
-        t -= consumed;
-        if (consumed == 0) {
-          if (++idle_rounds > p.spin_limit) {
-            atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
-            break;
-          }
-          __nanosleep(LB_SLEEP_NS);
-          win = 1;
-        } else {
-          win = LB_WIN;
-        }
-      }
-      st_relaxed(status + tid, make_status(FLAG_INC, gen, prefix + unit_count));
-    }
-    if constexpr (CLUSTER > 1) s_prefix[tid] = prefix;
-  }
-  if constexpr (CLUSTER > 1) {
-    cluster_sync();
-    if (tid < RADIX) prefix = cg::this_cluster().map_shared_rank(s_prefix, 0)[tid];
-    cluster_arrive();  // the first CTA's s_prefix stays valid until all have read it
-  }
-  if (tid < RADIX) {
-    const uint32_t bb = p.seg_binbase != nullptr
-                            ? p.seg_binbase[(size_t(seg) * p.seg_digits + p.pass) * RADIX + tid]
-                            : plan.binbase[p.pass][tid];
-    s_dst_base[tid] = uint32_t(e0) + bb + prefix + cl_excl - tile_excl;
-    // This CTA writes the digit's elements to [e0 + bb + prefix + cl_excl,
-    // + count): the range is checked once per digit, not per element.
-    if (count != 0 && uint64_t(e0) + bb + prefix + cl_excl + count > e1) {
-      s_bad = 1;
-      atomicOr(p.err, ERR_SCATTER_RANGE);
-    }
-    if (unstable) {
-      s_offd[0][tid] = uint16_t(tile_excl);
+    };
+    if constexpr (THREADS >= 2 * RADIX) {
+      if (tid >= RADIX && tid < 2 * RADIX) write_offsets(uint32_t(tid - RADIX));
     } else {
-#pragma unroll
-      for (int w = 0; w < WARPS; ++w) s_offd[w][tid] = uint16_t(s_offd[w][tid] + tile_excl);
+      if (tid < RADIX) write_offsets(uint32_t(tid));
     }
-  }
-  __syncthreads();
 
-  // Reorder the tile in shared memory by digit (keys in transformed form).
-  K* s_keys = reinterpret_cast<K*>(s_dyn);
-  VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
-  uint8_t* s_bdig = s_dyn + Cfg::DYN_SMEM;  // BUCKET mode only
-  const uint16_t* s_off = s_offd[unstable ? 0 : warp];
+    // Decoupled look-back over preceding tiles, LB_WIN words per round,
+    // bounded by spin_limit rounds without progress. While the nearest word
+    // is pending, one word is polled per round after a short sleep, so
+    // waiting warps leave issue slots and L1 bandwidth to the tiles they
+    // wait for.
+    uint32_t prefix = 0;
+    if (tid < RADIX) {
+      if (tile > first_unit) {
+        int64_t t = int64_t(tile) - 1;
+        uint32_t idle_rounds = 0;
+        const bool stall = p.inject_stall && tile == 1;
+        int win = LB_WIN;
+        while (true) {
+          uint64_t w[LB_WIN];
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    if (wloc + 32 * i < tile_n) {
-      const uint32_t d = digit_at(i);
-      const uint32_t start = s_off[d];
-      const uint32_t pos = start + get_rank(i);
-      s_keys[pos] = keys[i];
-      if constexpr (HAS_V) s_vals[pos] = vals[i];
-      if constexpr (BUCKET) s_bdig[pos] = uint8_t(d);
-    }
-  }
-  __syncthreads();
-
-  // Scatter: consecutive tile positions of one digit go to consecutive
-  // output addresses.
-  const uint32_t n_ok = s_bad ? 0u : tile_n;  // a tile that failed the check writes nothing
+          for (int k = 0; k < LB_WIN; ++k) {
+            const int64_t tt = t - k;
+            w[k] = (k < win && tt >= 0 && !stall) ? ld_relaxed(p.status + uint64_t(tt) * RADIX + tid)
+                                                  : 0ull;
+          }
+          int consumed = 0;
+          bool done = false;
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const uint32_t r = uint32_t(i) * THREADS + tid;
-    if (r < n_ok) {
-      const K k = s_keys[r];
-      uint32_t d;
-      VS v;
-      if constexpr (HAS_V) {
-        v = s_vals[r];
-        d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1)) : key_digit(k);
-      } else if constexpr (BUCKET) {
-        d = s_bdig[r];
-      } else {
-        d = key_digit(k);
+          for (int k = 0; k < LB_WIN; ++k) {
+            const uint64_t wk = w[k];
+            const bool ready = (wk & FLAG_MASK) != 0 && uint32_t((wk >> 32) & GEN_MASK) == gen;
+            if (!done && consumed == k && ready) {
+              prefix += uint32_t(wk);
+              consumed = k + 1;
+              done = (wk & FLAG_MASK) == FLAG_INC;
+            }
+          }
+          if (done) break;
+          t -= consumed;
+          if (consumed == 0) {
+            if (++idle_rounds > p.spin_limit) {
+              atomicOr(p.err, ERR_LOOKBACK_TIMEOUT);
+              break;
+            }
+            __nanosleep(LB_SLEEP_NS);
+            win = 1;
+          } else {
+            win = LB_WIN;
+          }
+        }
+        st_relaxed(status + tid, make_status(FLAG_INC, gen, prefix + count));
       }
-      const uint32_t dst = s_dst_base[d] + r;
-      dst_k[dst] = last ? kx.inv(k) : k;
-      if constexpr (HAS_V) dst_v[dst] = v;
+      const uint32_t bb = p.seg_binbase != nullptr
+                              ? p.seg_binbase[(size_t(seg) * p.seg_digits + p.pass) * RADIX + tid]
+                              : plan.binbase[p.pass][tid];
+      s_dst_base[tid] = uint32_t(e0) + bb + prefix - tile_excl;
+      // This tile writes the digit's elements to [e0 + bb + prefix, + count):
+      // the range is checked once per digit, not per element.
+      if (count != 0 && uint64_t(e0) + bb + prefix + count > e1) {
+        s_bad = 1;
+        atomicOr(p.err, ERR_SCATTER_RANGE);
+      }
     }
-  }
-  if constexpr (CLUSTER > 1) cluster_wait();
+    __syncthreads();
+
+    // Reorder the tile in shared memory by digit (keys in transformed form).
+    K* s_keys = reinterpret_cast<K*>(s_dyn);
+    VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
+    uint8_t* s_bdig = s_dyn + Cfg::DYN_SMEM;  // BUCKET mode only
+    const OffT* s_off = s_offd[unstable ? 0 : warp];
+    const uint32_t hsh = RANK == RANK_HALF ? 16u * (uint32_t(lane) >> 4) : 0u;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      if (in_tile(wloc + STRIDE * i)) {
+        const uint32_t d = digit_at(i);
+        const uint32_t pos = ((uint32_t(s_off[d]) >> hsh) & 0xFFFFu) + get_rank(i);
+        s_keys[pos] = keys[i];
+        if constexpr (HAS_V) s_vals[pos] = vals[i];
+        if constexpr (BUCKET) s_bdig[pos] = uint8_t(d);
+      }
+    }
+    __syncthreads();
+
+    // Scatter: consecutive tile positions of one digit go to consecutive
+    // output addresses. A tile that failed the range check writes nothing.
+    auto scatter = [&](auto last_c) {
+      constexpr bool LAST = decltype(last_c)::value;
+      if (s_bad) return;
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t r = uint32_t(i) * THREADS + tid;
+        if (in_tile(r)) {
+          const K k = s_keys[r];
+          uint32_t d;
+          VS v;
+          if constexpr (HAS_V) {
+            v = s_vals[r];
+            d = from_val ? (uint32_t(vx.fwd(v) >> shift) & (RADIX - 1)) : key_digit(k);
+          } else if constexpr (BUCKET) {
+            d = s_bdig[r];
+          } else {
+            d = key_digit(k);
+          }
+          const uint32_t dst = s_dst_base[d] + r;
+          dst_k[dst] = LAST ? kx.inv(k) : k;
+          if constexpr (HAS_V) dst_v[dst] = v;
+        }
+      }
+    };
+    if (last) scatter(std::true_type{});
+    else scatter(std::false_type{});
+  };
+  if (tile_n == uint32_t(TILE)) body(std::true_type{});
+  else body(std::false_type{});
 }
 
 }  // namespace gs

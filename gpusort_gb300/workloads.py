@@ -1,8 +1,9 @@
-"""Single runs of each sort path on synthetic uniform keys, for profiling the
-kernels one path launches:
+"""Profiling helper (not part of the sort API): single runs of each sort path
+on synthetic uniform keys, so that a profiler sees only the kernels one path
+launches. The ncu summaries of the kernels are made with it:
 
     python -m gpusort_gb300.workloads {radix,pairs,hyk,sample,segmented,gather,host}
-        [--log2n N] [--runs R]
+        [--log2n N] [--runs R] [--shape S]
 
 * radix      - gs_sort_keys, onesweep radix (upsweep, plan, passes)
 * pairs      - gs_sort_pairs, uint64 Zipf(1.1) keys with a uint32 index
@@ -20,7 +21,8 @@ kernels one path launches:
                arrives
 
 Each run is synchronous and checked for GS_OK; `--runs` (default 2) lets a
-profiler skip the first run's launches.
+profiler skip the first run's launches. `--shape` selects the pass kernel's
+tile shape (gs_pass_shape_info) instead of the default by size.
 """
 from __future__ import annotations
 
@@ -37,10 +39,13 @@ def main(argv=None):
                                      "host"])
     ap.add_argument("--log2n", type=int, default=26)
     ap.add_argument("--runs", type=int, default=2)
+    ap.add_argument("--shape", type=int, default=-1)
     args = ap.parse_args(argv)
     import torch
     ctx = capi.Context(0)
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    if args.shape >= 0:
+        ctx.debug_set(capi.DEBUG_PASS_SHAPE, args.shape)
     n = 1 << args.log2n
     a = datagen.device("uniform", n, np.uint32, seed=1)
     o = torch.empty_like(a)

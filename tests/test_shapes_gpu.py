@@ -44,6 +44,30 @@ def test_hyk_sort_shape(ctx, dtype, dist):
             assert same_bits(got, oracle.sort_keys(a, desc)), (n, p, k, desc)
 
 
+@pytest.mark.parametrize("p", [4, 16, 64])
+@pytest.mark.parametrize("k", [2, 4, 8])
+@pytest.mark.parametrize("dtype", [np.uint32, np.float64])
+def test_hyk_rounds_p_by_k(ctx, p, k, dtype):
+    """log_k(p) rounds of splitter selection, cuts and one k-way merge each
+    (k reduced to the group size in the last round when k does not divide
+    the group evenly in powers)."""
+    for dist in ("uniform", "zipf", "distinct8", "equal", "sorted"):
+        for n in (p * 3 + 1, 200_003):
+            a = datagen.host(dist, n, dtype, seed=n + p * 7 + k)
+            for desc in (False, True):
+                got = _run(ctx, a, capi.ALGO_HYK, desc, in_place=desc, partitions=p,
+                           k_way=k, seed=p + k)
+                assert same_bits(got, oracle.sort_keys(a, desc)), (dist, n, p, k, desc)
+
+
+def test_hyk_large_groups(ctx):
+    """256 partitions with 16-way rounds, and 512 partitions 2-way."""
+    for p, k, n in ((256, 16, 1 << 20), (512, 2, 300_001)):
+        a = datagen.host("uniform", n, np.uint64, seed=p)
+        got = _run(ctx, a, capi.ALGO_HYK, False, partitions=p, k_way=k)
+        assert same_bits(got, oracle.sort_keys(a)), (p, k)
+
+
 def test_shapes_on_reference_rank_config(ctx):
     """The reference's CPU case: 4 ranks x 2^20 uint32, HykSort k=4."""
     a = np.concatenate([datagen.host("uniform", 1 << 20, np.uint32, seed=0x67707573 + r)
