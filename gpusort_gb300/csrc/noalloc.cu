@@ -24,14 +24,15 @@
 namespace {
 
 constexpr uint64_t kMaxKeys = GS_NOALLOC_MAX_KEYS;           // 2^20 keys
-constexpr uint32_t kTile = 8192;                              // u32 pass tile
+constexpr uint32_t kTile = gs::RADIX_TILE_U32_SHAPE0;         // keys per pass tile
 constexpr size_t kAltBytes = size_t(kMaxKeys) * 4;            // ping-pong keys
+// One look-back word per tile and digit.
 constexpr size_t kStatusBytes = size_t((kMaxKeys + kTile - 1) / kTile) * gs::RADIX * 8;
 constexpr size_t kWorkBytes = (sizeof(gs::SortWork) + 255) / 256 * 256;
 constexpr size_t kErrBytes = 256;
 constexpr size_t kScratchBytes = kAltBytes + kStatusBytes + kWorkBytes + kErrBytes;
 
-// The shared scratch of every call on this device (about 4.3 MB). Host code
+// The shared scratch of every call on this device (about 4.2 MB). Host code
 // must not use this name as an address: it is the host-side shadow of the
 // symbol. The device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -52,13 +53,20 @@ gs_status fail(gs_status st, const std::string& msg) {
 }
 
 // Once per device, with that device current: find the array's device
-// address and clear the look-back words (the tags there must start at 0).
+// address and clear the look-back words and the work area (the look-back
+// tags are drawn from a counter there, which must start at 0). cudaMemset
+// is asynchronous and runs on the legacy default stream, which a
+// non-blocking caller stream does not wait for, so the set-up waits for the
+// device: the clear is done before the first sort is enqueued on any stream.
+// This is why the first call on a device must not come during a stream
+// capture.
 void setup(int dev, DeviceSlot& s) {
   void* p = nullptr;
   s.setup_err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (s.setup_err != cudaSuccess) return;
   s.scratch = static_cast<unsigned char*>(p);
   s.setup_err = cudaMemset(s.scratch + kAltBytes, 0, kStatusBytes + kWorkBytes);
+  if (s.setup_err == cudaSuccess) s.setup_err = cudaDeviceSynchronize();
   if (s.setup_err != cudaSuccess) return;
   s.props.device = dev;
   cudaDeviceGetAttribute(&s.props.num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -99,6 +107,15 @@ gs_status gs_sort_keys_noalloc(gs_dtype dtype, const void* in, void* out, uint64
     return fail(GS_ERR_CUDA, std::string("no-alloc scratch set-up: ") +
                                  cudaGetErrorString(s.setup_err));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n <= gs::small_sort_max()) {
+    // One CTA sorts in its shared memory: no scratch at all.
+    cudaError_t e = gs::launch_small_sort(in, out, uint32_t(n), 4, kind,
+                                          (flags & GS_FLAG_DESCENDING) != 0, st);
+    if (e == cudaSuccess && (flags & GS_FLAG_SYNC)) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(GS_ERR_CUDA, std::string("small sort: ") +
+                                                       cudaGetErrorString(e));
+    return GS_OK;
+  }
   unsigned char* base = s.scratch;
   gs::RadixJob job;
   job.keys_in = in;

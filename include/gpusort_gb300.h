@@ -272,14 +272,17 @@ gs_status gs_ctx_choice(gs_ctx* ctx, gs_dtype key_dtype, int val_bytes, uint64_t
  * allocator owns the device memory, latency-critical paths where
  * cudaMalloc/cudaFree would synchronise the device, plugins whose host
  * forbids allocation after start-up.
- * - Scratch is one fixed device array inside the library (about 4.3 MB per
+ * - Scratch is one fixed device array inside the library (about 4.2 MiB per
  *   GPU that loads it, held until the process exits). n may be at most
- *   GS_NOALLOC_MAX_KEYS; larger n returns GS_ERR_TOO_LARGE.
+ *   GS_NOALLOC_MAX_KEYS; larger n returns GS_ERR_TOO_LARGE. Up to 4096
+ *   keys are sorted in one CTA's shared memory and use no scratch.
  * - The caller passes device input and output (they may alias) and a CUDA
  *   stream (NULL: the legacy default stream). Flags: GS_FLAG_DESCENDING,
  *   and GS_FLAG_SYNC to wait and report GS_ERR_TIMEOUT.
- * - The first call on a device sets up that device's scratch address (and
- *   clears it); make that first call before any stream capture.
+ * - The first call on a device sets up that device's scratch address and
+ *   clears it, waiting for the device (cudaDeviceSynchronize) so that the
+ *   clear is done before any sort on any stream; make that first call
+ *   before any stream capture.
  * - Every call on a device shares the one scratch array: calls that overlap
  *   on the GPU (other streams, other threads) race and corrupt each other.
  * - Errors are described by gs_last_global_error(). */
