@@ -11,9 +11,12 @@
 //    std::less<T> or std::greater<T> (include/helpers/hyksort_helper.h:
 //    94-145 local sort + SortAmongProcesses 453-536; include/omp/
 //    omp_utils.h:147-207 MergeSort; include/common.h:156-164 ConvertComp).
-//    A sorted multiset is unique, so std::sort reproduces it bit for bit
-//    (given no NaN; -0.0 and +0.0 compare equal, so keys-only inputs avoid
-//    -0.0, and pair inputs holding both zeros have distinct values).
+//    A sorted multiset is unique, so std::sort, or the parallel merge sort
+//    of the reference's OpenMP local sort (p parts, std::sort each, tree of
+//    2-way merges), reproduces it bit for bit (given no NaN; -0.0 and +0.0
+//    compare equal, so keys-only inputs avoid -0.0, and pair inputs holding
+//    both zeros have distinct values). Large inputs use that parallel form
+//    on every host core, so full-size outputs are checked in seconds.
 //
 //  * oracle_sort_pairs: the CPU key/value path sorts std::pair<K,V> with
 //    ConvertComp<pair>(comp), i.e. lexicographic (key, value) order, both
@@ -49,32 +52,37 @@ namespace {
 
 enum Dtype { U32 = 0, I32 = 1, F32 = 2, U64 = 3, I64 = 4, F64 = 5 };
 
+template <typename T, typename Cmp>
+void par_sort(T* v, int64_t n, int threads, Cmp cmp, bool stable);
+
+// Keys: the sorted multiset under std::less / std::greater, by the parallel
+// merge sort below (`threads` workers; one worker is plain std::sort).
 template <typename T>
-void sort_keys_t(const void* in, void* out, uint64_t n, bool desc) {
+void sort_keys_t(const void* in, void* out, uint64_t n, bool desc, int threads) {
   const T* a = static_cast<const T*>(in);
   T* b = static_cast<T*>(out);
   if (a != b) std::memcpy(b, a, n * sizeof(T));
-  if (desc) std::sort(b, b + n, std::greater<T>());
-  else std::sort(b, b + n, std::less<T>());
+  if (desc) par_sort(b, int64_t(n), threads, std::greater<T>(), false);
+  else par_sort(b, int64_t(n), threads, std::less<T>(), false);
 }
 
 template <typename K, typename V>
 void sort_pairs_t(const void* kin, const void* vin, void* kout, void* vout, uint64_t n,
-                  bool desc, bool stable) {
+                  bool desc, bool stable, int threads) {
   const K* k = static_cast<const K*>(kin);
   const V* v = static_cast<const V*>(vin);
   std::vector<std::pair<K, V>> items(n);
   for (uint64_t i = 0; i < n; ++i) items[i] = std::make_pair(k[i], v[i]);
+  std::pair<K, V>* it = items.data();
   if (stable) {
-    std::stable_sort(items.begin(), items.end(),
-                     [](const std::pair<K, V>& a, const std::pair<K, V>& b) {
-                       return a.first < b.first;
-                     });
+    par_sort(it, int64_t(n), threads,
+             [](const std::pair<K, V>& a, const std::pair<K, V>& b) { return a.first < b.first; },
+             true);
     if (desc) std::reverse(items.begin(), items.end());
   } else if (desc) {
-    std::sort(items.begin(), items.end(), std::greater<std::pair<K, V>>());
+    par_sort(it, int64_t(n), threads, std::greater<std::pair<K, V>>(), false);
   } else {
-    std::sort(items.begin(), items.end(), std::less<std::pair<K, V>>());
+    par_sort(it, int64_t(n), threads, std::less<std::pair<K, V>>(), false);
   }
   K* ko = static_cast<K*>(kout);
   V* vo = static_cast<V*>(vout);
@@ -86,14 +94,14 @@ void sort_pairs_t(const void* kin, const void* vin, void* kout, void* vout, uint
 
 template <typename K>
 bool dispatch_v(int vt, const void* kin, const void* vin, void* kout, void* vout, uint64_t n,
-                bool desc, bool stable) {
+                bool desc, bool stable, int th) {
   switch (vt) {
-    case U32: sort_pairs_t<K, uint32_t>(kin, vin, kout, vout, n, desc, stable); return true;
-    case I32: sort_pairs_t<K, int32_t>(kin, vin, kout, vout, n, desc, stable); return true;
-    case F32: sort_pairs_t<K, float>(kin, vin, kout, vout, n, desc, stable); return true;
-    case U64: sort_pairs_t<K, uint64_t>(kin, vin, kout, vout, n, desc, stable); return true;
-    case I64: sort_pairs_t<K, int64_t>(kin, vin, kout, vout, n, desc, stable); return true;
-    case F64: sort_pairs_t<K, double>(kin, vin, kout, vout, n, desc, stable); return true;
+    case U32: sort_pairs_t<K, uint32_t>(kin, vin, kout, vout, n, desc, stable, th); return true;
+    case I32: sort_pairs_t<K, int32_t>(kin, vin, kout, vout, n, desc, stable, th); return true;
+    case F32: sort_pairs_t<K, float>(kin, vin, kout, vout, n, desc, stable, th); return true;
+    case U64: sort_pairs_t<K, uint64_t>(kin, vin, kout, vout, n, desc, stable, th); return true;
+    case I64: sort_pairs_t<K, int64_t>(kin, vin, kout, vout, n, desc, stable, th); return true;
+    case F64: sort_pairs_t<K, double>(kin, vin, kout, vout, n, desc, stable, th); return true;
   }
   return false;
 }
@@ -135,13 +143,16 @@ void par_merge(const T* a, int64_t na, const T* b, int64_t nb, T* out, int threa
   for (auto& w : ws) w.join();
 }
 
-// Local merge sort of one rank (include/omp/omp_utils.h:147-207): split in
-// `threads` parts, std::sort each, merge pairs level by level.
+// Parallel merge sort (include/omp/omp_utils.h:147-207 MergeSort): split in
+// `threads` parts, sort each (std::sort, or std::stable_sort when `stable`),
+// then merge pairs of runs level by level with the parallel 2-way merge.
+// std::merge and the merge-path split take ties from the left run first, so
+// the stable variant stays stable.
 template <typename T, typename Cmp>
-void local_merge_sort(std::vector<T>& v, int threads, Cmp cmp) {
-  const int64_t n = int64_t(v.size());
-  if (threads <= 1 || n < 2 * threads) {
-    std::sort(v.begin(), v.end(), cmp);
+void par_sort(T* v, int64_t n, int threads, Cmp cmp, bool stable) {
+  if (threads <= 1 || n < 65536 || n < 2 * threads) {
+    if (stable) std::stable_sort(v, v + n, cmp);
+    else std::sort(v, v + n, cmp);
     return;
   }
   std::vector<int64_t> split(threads + 1);
@@ -149,11 +160,14 @@ void local_merge_sort(std::vector<T>& v, int threads, Cmp cmp) {
   {
     std::vector<std::thread> ws;
     for (int i = 0; i < threads; ++i)
-      ws.emplace_back([&, i] { std::sort(v.begin() + split[i], v.begin() + split[i + 1], cmp); });
+      ws.emplace_back([&, i] {
+        if (stable) std::stable_sort(v + split[i], v + split[i + 1], cmp);
+        else std::sort(v + split[i], v + split[i + 1], cmp);
+      });
     for (auto& w : ws) w.join();
   }
   std::vector<T> buf(n);
-  T* a = v.data();
+  T* a = v;
   T* b = buf.data();
   for (int j = 1; j < threads; j *= 2) {
     for (int i = 0; i < threads; i += 2 * j) {
@@ -167,7 +181,13 @@ void local_merge_sort(std::vector<T>& v, int threads, Cmp cmp) {
     }
     std::swap(a, b);
   }
-  if (a != v.data()) std::copy(a, a + n, v.data());
+  if (a != v) std::copy(a, a + n, v);
+}
+
+// Local merge sort of one rank of the HykSort port.
+template <typename T, typename Cmp>
+void local_merge_sort(std::vector<T>& v, int threads, Cmp cmp) {
+  par_sort(v.data(), int64_t(v.size()), threads, cmp, false);
 }
 
 template <typename T, typename Cmp>
@@ -362,44 +382,54 @@ bool is_pow2(unsigned v) { return v && !(v & (v - 1)); }
 
 extern "C" {
 
-int oracle_sort_keys(int dtype, const void* in, void* out, uint64_t n, int desc) {
+// `threads` workers (<= 1: one).
+int oracle_sort_keys(int dtype, const void* in, void* out, uint64_t n, int desc, int threads) {
   switch (dtype) {
-    case U32: sort_keys_t<uint32_t>(in, out, n, desc); return 0;
-    case I32: sort_keys_t<int32_t>(in, out, n, desc); return 0;
-    case F32: sort_keys_t<float>(in, out, n, desc); return 0;
-    case U64: sort_keys_t<uint64_t>(in, out, n, desc); return 0;
-    case I64: sort_keys_t<int64_t>(in, out, n, desc); return 0;
-    case F64: sort_keys_t<double>(in, out, n, desc); return 0;
+    case U32: sort_keys_t<uint32_t>(in, out, n, desc, threads); return 0;
+    case I32: sort_keys_t<int32_t>(in, out, n, desc, threads); return 0;
+    case F32: sort_keys_t<float>(in, out, n, desc, threads); return 0;
+    case U64: sort_keys_t<uint64_t>(in, out, n, desc, threads); return 0;
+    case I64: sort_keys_t<int64_t>(in, out, n, desc, threads); return 0;
+    case F64: sort_keys_t<double>(in, out, n, desc, threads); return 0;
   }
   return -1;
 }
 
 int oracle_sort_pairs(int kt, int vt, const void* kin, const void* vin, void* kout, void* vout,
-                      uint64_t n, int desc, int stable) {
+                      uint64_t n, int desc, int stable, int threads) {
   bool ok = false;
   switch (kt) {
-    case U32: ok = dispatch_v<uint32_t>(vt, kin, vin, kout, vout, n, desc, stable); break;
-    case I32: ok = dispatch_v<int32_t>(vt, kin, vin, kout, vout, n, desc, stable); break;
-    case F32: ok = dispatch_v<float>(vt, kin, vin, kout, vout, n, desc, stable); break;
-    case U64: ok = dispatch_v<uint64_t>(vt, kin, vin, kout, vout, n, desc, stable); break;
-    case I64: ok = dispatch_v<int64_t>(vt, kin, vin, kout, vout, n, desc, stable); break;
-    case F64: ok = dispatch_v<double>(vt, kin, vin, kout, vout, n, desc, stable); break;
+    case U32: ok = dispatch_v<uint32_t>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
+    case I32: ok = dispatch_v<int32_t>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
+    case F32: ok = dispatch_v<float>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
+    case U64: ok = dispatch_v<uint64_t>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
+    case I64: ok = dispatch_v<int64_t>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
+    case F64: ok = dispatch_v<double>(vt, kin, vin, kout, vout, n, desc, stable, threads); break;
   }
   return ok ? 0 : -1;
 }
 
 // Batched sort: each segment [off[s], off[s+1]) sorted on its own, as each
-// rank's local sort is (include/omp/omp_utils.h:147-207).
+// rank's local sort is (include/omp/omp_utils.h:147-207); `threads` workers
+// take segments in turn.
 int oracle_segmented_sort_keys(int dtype, const void* in, void* out, uint64_t n,
-                               const uint64_t* off, uint32_t nseg, int desc) {
+                               const uint64_t* off, uint32_t nseg, int desc, int threads) {
+  if (dtype < U32 || dtype > F64) return -1;
   const size_t eb = (dtype <= F32) ? 4 : 8;
   if (in != out) std::memcpy(out, in, n * eb);
   uint8_t* base = static_cast<uint8_t*>(out);
-  for (uint32_t s = 0; s < nseg; ++s) {
-    const uint64_t b = off[s], e = off[s + 1];
-    if (e <= b) continue;
-    if (oracle_sort_keys(dtype, base + b * eb, base + b * eb, e - b, desc) != 0) return -1;
-  }
+  std::atomic<uint32_t> next{0};
+  auto work = [&] {
+    for (uint32_t s = next++; s < nseg; s = next++) {
+      const uint64_t b = off[s], e = off[s + 1];
+      if (e > b) oracle_sort_keys(dtype, base + b * eb, base + b * eb, e - b, desc, 1);
+    }
+  };
+  const int t = threads < 1 ? 1 : threads;
+  std::vector<std::thread> ws;
+  for (int i = 1; i < t; ++i) ws.emplace_back(work);
+  work();
+  for (auto& w : ws) w.join();
   return 0;
 }
 

@@ -39,10 +39,10 @@ def _load():
             build()
         L = C.CDLL(str(LIB))
         vp, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
-        L.oracle_sort_keys.argtypes = [i32, vp, vp, u64, i32]
-        L.oracle_sort_pairs.argtypes = [i32, i32, vp, vp, vp, vp, u64, i32, i32]
+        L.oracle_sort_keys.argtypes = [i32, vp, vp, u64, i32, i32]
+        L.oracle_sort_pairs.argtypes = [i32, i32, vp, vp, vp, vp, u64, i32, i32, i32]
         L.oracle_hyksort_cpu.argtypes = [i32, vp, u64, i32, i32, i32, u64, i32]
-        L.oracle_segmented_sort_keys.argtypes = [i32, vp, vp, u64, vp, C.c_uint32, i32]
+        L.oracle_segmented_sort_keys.argtypes = [i32, vp, vp, u64, vp, C.c_uint32, i32, i32]
         for f in ("oracle_sort_keys", "oracle_sort_pairs", "oracle_hyksort_cpu",
                   "oracle_segmented_sort_keys"):
             getattr(L, f).restype = i32
@@ -50,37 +50,43 @@ def _load():
     return _lib
 
 
-def sort_keys(keys: np.ndarray, descending: bool = False) -> np.ndarray:
+def _threads(threads: int | None) -> int:
+    """Worker threads of one oracle call: every host core unless given."""
+    return max(1, int(threads if threads is not None else (os.cpu_count() or 1)))
+
+
+def sort_keys(keys: np.ndarray, descending: bool = False, threads: int | None = None) -> np.ndarray:
     """Globally sorted copy under std::less / std::greater."""
     a = np.ascontiguousarray(keys)
     out = np.empty_like(a)
     rc = _load().oracle_sort_keys(_CODES[a.dtype], a.ctypes.data, out.ctypes.data, a.size,
-                                  int(descending))
+                                  int(descending), _threads(threads))
     assert rc == 0
     return out
 
 
 def sort_pairs(keys: np.ndarray, vals: np.ndarray, descending: bool = False,
-               stable: bool = False) -> tuple[np.ndarray, np.ndarray]:
+               stable: bool = False, threads: int | None = None) -> tuple[np.ndarray, np.ndarray]:
     """(key, value) order of the reference's CPU pair path, or stable-by-key."""
     k = np.ascontiguousarray(keys)
     v = np.ascontiguousarray(vals)
     ko, vo = np.empty_like(k), np.empty_like(v)
     rc = _load().oracle_sort_pairs(_CODES[k.dtype], _CODES[v.dtype], k.ctypes.data,
                                    v.ctypes.data, ko.ctypes.data, vo.ctypes.data, k.size,
-                                   int(descending), int(stable))
+                                   int(descending), int(stable), _threads(threads))
     assert rc == 0
     return ko, vo
 
 
 def segmented_sort_keys(keys: np.ndarray, offsets: np.ndarray,
-                        descending: bool = False) -> np.ndarray:
+                        descending: bool = False, threads: int | None = None) -> np.ndarray:
     """Each segment [offsets[s], offsets[s+1]) sorted on its own."""
     a = np.ascontiguousarray(keys)
     off = np.ascontiguousarray(offsets, dtype=np.uint64)
     out = np.empty_like(a)
     rc = _load().oracle_segmented_sort_keys(_CODES[a.dtype], a.ctypes.data, out.ctypes.data,
-                                            a.size, off.ctypes.data, off.size - 1, int(descending))
+                                            a.size, off.ctypes.data, off.size - 1, int(descending),
+                                            _threads(threads))
     assert rc == 0
     return out
 
