@@ -87,7 +87,7 @@ bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads
 int radix_default_shape(int key_bytes, int val_bytes, uint64_t n);
 // Tile (keys) of shape 0 for 32-bit keys without payload, and the look-back
 // words of a job run with that shape.
-constexpr uint32_t RADIX_TILE_U32_SHAPE0 = 512 * 24;
+constexpr uint32_t RADIX_TILE_U32_SHAPE0 = 384 * 24;
 size_t radix_status_words_u32_shape0(uint64_t n);
 // Look-back words a job of n elements needs.
 size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);

@@ -78,28 +78,38 @@ constexpr int UPSWEEP_PER_SM = 3;
 
 // Tile shapes of the pass kernel (threads per block, items per thread,
 // blocks per SM, ranking of the stable passes), selectable per call; shape
-// 0 is the default. Larger elements take fewer items per thread. Shapes 0
-// and 2 share a geometry and differ in the ranking: half-warp ranking is
-// faster for keys (2^30 u32: 16.0 vs 16.8 ms; 2^29 u64: 24.7 vs 25.7 ms),
-// the 64-bit table for key/value pairs (2^29 u64 + u32: 56.0 vs 56.6 ms).
+// 0 is the default. Larger elements take fewer items per thread: each
+// shape has the most items that fit its register share without spilling
+// (or with a few bytes of spill where that measured faster).
+//  - Shape 0: 384 threads, 3 CTAs per SM. More CTAs per SM hide more of
+//    each tile's barrier and look-back latency than 512-thread tiles at 2
+//    CTAs per SM: 2^30 u32 keys 14.7 vs 15.4 ms, 2^29 u64 23.4 vs 23.9 ms,
+//    2^29 u64 + u32 pairs 53.4 vs 55.2 ms, u32 + u32 26.9 vs 27.7 ms.
+//    (320 x 24 x 3: 15.7 ms; 256 x 24 x 4: 16.4 ms; 384 x 22 x 3: 15.1 ms;
+//    384 x 32 x 2: 15.1 ms.) 64-bit keys with 64-bit payloads spill at 384
+//    threads and keep 512.
+//  - Shape 1: 256 threads, 4 CTAs per SM, for small sorts.
+//  - Shape 2: 512 threads, 2 CTAs per SM (the previous default).
+// Keys rank by half-warps (2^30 u32: stable passes 3.97 vs 4.30 ms with the
+// 64-bit table), pairs by the table (2^29 u64 + u32: 56.0 vs 56.6 ms).
 template <int T, int I, int B, int R = RANK_TABLE> struct Shape {
   static constexpr int THREADS = T, ITEMS = I, MINB = B, RANK = R;
 };
 template <typename K, typename V, int S> struct PassShape;
-template <> struct PassShape<uint32_t, NoValue, 0> : Shape<512, 24, 2, RANK_HALF> {};
+template <> struct PassShape<uint32_t, NoValue, 0> : Shape<384, 24, 3, RANK_HALF> {};
 template <> struct PassShape<uint32_t, NoValue, 1> : Shape<256, 20, 4> {};
-template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 24, 2> {};
-template <> struct PassShape<uint64_t, NoValue, 0> : Shape<512, 14, 2, RANK_HALF> {};
+template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 24, 2, RANK_HALF> {};
+template <> struct PassShape<uint64_t, NoValue, 0> : Shape<384, 14, 3, RANK_HALF> {};
 template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4> {};
-template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 14, 2> {};
-template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<512, 14, 2> {};
+template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 14, 2, RANK_HALF> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<384, 14, 3> {};
 template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4> {};
-template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<512, 14, 2, RANK_HALF> {};
+template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<512, 14, 2> {};
 template <> struct PassShape<uint64_t, uint64_t, 0> : Shape<512, 9, 2> {};
 template <> struct PassShape<uint64_t, uint64_t, 2> : Shape<512, 9, 2, RANK_HALF> {};
 template <typename K, typename V, int S>
-struct PassShape : Shape<(S == 1 ? 256 : 512), (S == 1 ? 6 : 10), (S == 1 ? 4 : 2),
-                         (S == 2 ? RANK_HALF : RANK_TABLE)> {};
+struct PassShape : Shape<(S == 0 ? 384 : S == 1 ? 256 : 512), (S == 1 ? 6 : 10),
+                         (S == 0 ? 3 : S == 1 ? 4 : 2), RANK_TABLE> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 1024;  // no shape has a smaller tile (smallest: 256 x 6)
 
@@ -306,7 +316,7 @@ int radix_segmented_shape(int key_bytes, uint64_t n, uint32_t nseg) {
   // (100,000 segments of 16 .. 2^22 keys, ~2^30 in all: 23.0 ms vs 23.8 ms
   // with 512 x 24 tiles, which leave more of each segment's last tile
   // empty). Few large segments (the SampleSort and HykSort shapes' buckets
-  // and partitions): the plain sort's 512-thread shape.
+  // and partitions): the plain sort's default shape 0.
   (void)key_bytes;
   return nseg != 0 && n / nseg >= (uint64_t(1) << 20) ? 0 : 1;
 }
@@ -421,13 +431,10 @@ bool radix_shape_info(int key_bytes, int val_bytes, int shape, uint32_t* threads
   return true;
 }
 
-// Measured defaults on GB300 (uniform keys, 2^22..2^30): the 512-thread
-// shape is fastest for every key and value width; its items per thread are
-// the most that fit 64 registers without spilling (u32 keys 512 x 24: 2^29
-// in 9.40 ms vs 10.71 at 16 items; u64 keys 512 x 14: 26.99 vs 28.57 ms at
-// 12; u64 + u32 pairs 512 x 10: 37.7 vs 41.7 ms at 8). Up to 2^18 keys
-// (no payload) a sort is a few tiles per pass and each pass takes about one
-// tile's latency, so the smaller 256-thread tiles win: 2^16 u32 keys 52.9 vs 65.0 us, u64 86.2 vs 102.7 us;
+// Measured defaults on GB300 (uniform keys, 2^22..2^30): shape 0 is
+// fastest for every key and value width (see the shape table). Up to 2^18
+// keys (no payload) a sort is a few tiles per pass and each pass takes
+// about one tile's latency, so the smaller 256-thread tiles win: 2^16 u32 keys 52.9 vs 65.0 us, u64 86.2 vs 102.7 us;
 // equal or worse from 2^20.
 int radix_default_shape(int key_bytes, int val_bytes, uint64_t n) {
   (void)key_bytes;

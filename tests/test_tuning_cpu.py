@@ -44,7 +44,7 @@ def test_pass_shapes_describe_threads_and_items(built_lib):
             shapes = capi.pass_shapes(kb, vb)
             assert len(shapes) == capi.load().gs_pass_shape_count() >= 2
             for t, it in shapes:
-                assert t in (256, 512) and 1 <= it <= 32
+                assert t in (256, 384, 512) and 1 <= it <= 32
     L = capi.load()
     assert L.gs_pass_shape_info(2, 0, 0, None, None) == capi.GS_ERR_INVALID
     assert L.gs_pass_shape_info(4, 0, 99, None, None) == capi.GS_ERR_INVALID
