@@ -333,7 +333,7 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
                b_pieces = size_t(p) * kmax * sizeof(gs::HykPiece);
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   st = ensure(ctx, ctx->hyk_small, al(b_roff) + al(b_split) + al(b_iters) + al(b_cuts) +
-                                       al(b_pieces));
+                                       al(b_pieces) + al(b_roff));
   if (st != GS_OK) return st;
   uint8_t* sm = static_cast<uint8_t*>(ctx->hyk_small.ptr);
   uint64_t* d_roff = reinterpret_cast<uint64_t*>(sm);
@@ -342,6 +342,9 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
   uint64_t* d_cuts = reinterpret_cast<uint64_t*>(sm + al(b_roff) + al(b_split) + al(b_iters));
   gs::HykPiece* d_pieces = reinterpret_cast<gs::HykPiece*>(sm + al(b_roff) + al(b_split) +
                                                             al(b_iters) + al(b_cuts));
+  uint64_t* d_rtile = reinterpret_cast<uint64_t*>(sm + al(b_roff) + al(b_split) + al(b_iters) +
+                                                  al(b_cuts) + al(b_pieces));
+  const uint64_t span = gs::hyk_tile_span(kb);
   const uint64_t seed = o ? o->seed : 0;
   uint32_t np = p;
   for (uint32_t round = 0; np > 1; ++round) {
@@ -394,17 +397,31 @@ gs_status hyk_sort_device(gs_ctx* ctx, int kb, uint32_t kk, const void* in, void
       noff[rr + 1] = noff[rr] + len;
     }
     if (noff[p] != n) return fail(ctx, GS_ERR_CUDA, "HykSort shape: pieces do not add up to n");
-    st = ensure(ctx, ctx->hyk_samples, size_t(std::max<uint64_t>(nsamples, 1)) * (16 + 8 * r.kway));
+    // Merge tiles: ceil(length / span) per receiving rank.
+    std::vector<uint64_t> rtile(p + 1, 0);
+    for (uint32_t rr = 0; rr < p; ++rr)
+      rtile[rr + 1] = rtile[rr] + (noff[rr + 1] - noff[rr] + span - 1) / span;
+    const uint64_t ntiles = rtile[p];
+    const size_t ns = size_t(nsamples), nt = size_t(ntiles), kw = r.kway;
+    st = ensure(ctx, ctx->hyk_samples, al(ns * 8) + al(ns * kw * 8) + al(nt * 8) +
+                                           al(nt * kw * 8) + al(nt * kw * 4) + 256);
     if (st != GS_OK) return st;
-    r.samp_rank = static_cast<uint64_t*>(ctx->hyk_samples.ptr);
-    r.samp_next = reinterpret_cast<int64_t*>(r.samp_rank + nsamples);
-    r.samp_cut = reinterpret_cast<uint64_t*>(r.samp_next + nsamples);
+    uint8_t* sp = static_cast<uint8_t*>(ctx->hyk_samples.ptr);
+    r.samp_rank = reinterpret_cast<uint64_t*>(sp);
+    r.samp_cut = reinterpret_cast<uint64_t*>(sp + al(ns * 8));
+    r.tile_out = reinterpret_cast<uint64_t*>(sp + al(ns * 8) + al(ns * kw * 8));
+    r.tile_src = reinterpret_cast<uint64_t*>(sp + al(ns * 8) + al(ns * kw * 8) + al(nt * 8));
+    r.tile_len = reinterpret_cast<uint32_t*>(sp + al(ns * 8) + al(ns * kw * 8) + al(nt * 8) +
+                                             al(nt * kw * 8));
+    r.err = ctx->err;
     e = cudaMemcpyAsync(d_pieces, pieces.data(), pieces.size() * sizeof(gs::HykPiece),
                         cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_rtile, rtile.data(), b_roff, cudaMemcpyHostToDevice, ctx->stream);
     void* next = cur == out ? alt : out;
     if (e == cudaSuccess)
-      e = gs::launch_hyk_merge(r, d_pieces, uint32_t(pieces.size()), nsamples, cur, next,
-                               ctx->stream);
+      e = gs::launch_hyk_merge(r, d_pieces, uint32_t(pieces.size()), nsamples, d_rtile, ntiles,
+                               cur, next, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // pieces and cuts are reused
     if (e != cudaSuccess) return cuda_fail(ctx, e, "k-way merge");
     phase_mark(ctx, "Merge data");

@@ -175,7 +175,10 @@ struct HykRound {
   uint64_t* cuts = nullptr;        // device, p x (kway + 1) cut offsets
   uint64_t* samp_rank = nullptr;   // device, per merge sample
   uint64_t* samp_cut = nullptr;    // device, per merge sample x kway
-  int64_t* samp_next = nullptr;    // device, per merge sample
+  uint64_t* tile_out = nullptr;    // device, per merge tile
+  uint64_t* tile_src = nullptr;    // device, per merge tile x kway
+  uint32_t* tile_len = nullptr;    // device, per merge tile x kway
+  uint32_t* err = nullptr;         // device error word
 };
 // One of the kway pieces a receiving rank merges: src .. src + len of the
 // source buffer; the rank's output starts at `out`; its pieces are
@@ -186,12 +189,17 @@ struct HykPiece {
   uint32_t first, j;
 };
 uint32_t hyk_sample_stride(int key_bytes, uint32_t kway);
+// Target tile length of the merge: a receiving rank of L elements has
+// ceil(L / hyk_tile_span) tiles.
+uint32_t hyk_tile_span(int key_bytes);
 size_t hyk_select_smem(int key_bytes, uint32_t n_p, uint32_t kway);
 // Splitter selection (one CTA per group) and the ranks' cut points.
 cudaError_t launch_hyk_select(const HykRound& r, cudaStream_t st);
-// The k-way merge of every receiving rank's pieces from src into dst.
+// The k-way merge of every receiving rank's pieces from src into dst;
+// rtile (device, p + 1) holds each receiving rank's first tile.
 cudaError_t launch_hyk_merge(const HykRound& r, const HykPiece* pieces, uint32_t npieces,
-                             uint64_t nsamples, const void* src, void* dst, cudaStream_t st);
+                             uint64_t nsamples, const uint64_t* rtile, uint64_t ntiles,
+                             const void* src, void* dst, cudaStream_t st);
 
 
 // Allow `kern` up to `bytes` of dynamic shared memory on the current device
