@@ -672,9 +672,9 @@ gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
   if (!host_offsets) return fail(ctx, GS_ERR_INVALID, "null offsets");
   cudaSetDevice(ctx->props.device);
   gs_seg_plan* pl = gs::seg_plan_new();
+  const int shape = ctx->shape >= 0 ? ctx->shape : gs::radix_segmented_shape(kb, n, nseg);
   const std::string err = gs::seg_plan_build(pl, host_offsets, nseg, n, kb, kk,
-                                             (flags & GS_FLAG_DESCENDING) != 0,
-                                             gs::radix_segmented_shape(kb, n, nseg));
+                                             (flags & GS_FLAG_DESCENDING) != 0, shape);
   if (!err.empty()) {
     gs::seg_plan_free(pl);
     return fail(ctx, err.find("allocation") != std::string::npos ? GS_ERR_OOM : GS_ERR_INVALID,

@@ -312,13 +312,13 @@ uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape) {
 }
 
 int radix_segmented_shape(int key_bytes, uint64_t n, uint32_t nseg) {
-  // Many moderate segments: the 256-thread shape
-  // (100,000 segments of 16 .. 2^22 keys, ~2^30 in all: 23.0 ms vs 23.8 ms
-  // with 512 x 24 tiles, which leave more of each segment's last tile
-  // empty). Few large segments (the SampleSort and HykSort shapes' buckets
-  // and partitions): the plain sort's default shape 0.
+  // Segments averaging at least 4096 keys (most keys in segments the passes
+  // sort): the default 384 x 24 shape. 100,000 segments of 16 .. 2^22 keys,
+  // ~2^30 in all: 19.7 ms vs 22.5 ms with the 256 x 20 shape and 21.3 ms
+  // with 512 x 24. Many short segments: the 256-thread shape, whose smaller
+  // tiles leave less of each segment's last tile empty.
   (void)key_bytes;
-  return nseg != 0 && n / nseg >= (uint64_t(1) << 20) ? 0 : 1;
+  return nseg != 0 && n / nseg >= 4096 ? 0 : 1;
 }
 
 cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const DeviceProps& props,
@@ -328,12 +328,14 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
     switch (job.shape) {
       case 0: return launch_passes<uint32_t, NoValue, 0>(job, &sj, digits, 0, props, gen, stream);
       case 1: return launch_passes<uint32_t, NoValue, 1>(job, &sj, digits, 0, props, gen, stream);
+      case 2: return launch_passes<uint32_t, NoValue, 2>(job, &sj, digits, 0, props, gen, stream);
       default: return cudaErrorInvalidValue;
     }
   }
   switch (job.shape) {
     case 0: return launch_passes<uint64_t, NoValue, 0>(job, &sj, digits, 0, props, gen, stream);
     case 1: return launch_passes<uint64_t, NoValue, 1>(job, &sj, digits, 0, props, gen, stream);
+    case 2: return launch_passes<uint64_t, NoValue, 2>(job, &sj, digits, 0, props, gen, stream);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -9,6 +9,11 @@
 //   shared memory and radix-sorts it by (local segment id, key) - an LSD
 //   sort over the key's digits and then the segment id - and writes it back
 //   in place of the group;
+// * tiny_sort_kernel: a group made only of segments of at most 32 keys is
+//   not radix-sorted; each of its segments is sorted by one warp with a
+//   bitonic network in registers (one key per lane, 15 compare-exchange
+//   stages by shuffles), so a 16-key segment no longer pays for LSD passes
+//   over a shared 4096-key tile;
 // * the onesweep pass kernel (radix.cuh) in its segmented form for larger
 //   segments: tiles never straddle segments, each segment has its own bin
 //   bases, and each segment's first tile starts its own look-back chain.
@@ -35,6 +40,41 @@ struct SegGroup {
   uint32_t nsegs;      // segments in the group (<= GROUP_MAX_SEGS)
   uint32_t pad;
 };
+
+constexpr uint32_t TINY_KEYS = 32;  // one key per lane of a warp
+
+struct TinySeg {
+  uint64_t start;
+  uint32_t len;  // 1 .. TINY_KEYS
+  uint32_t pad;
+};
+
+// One warp per segment of at most 32 keys: lane l holds key l (or the
+// largest order bits as padding) and a bitonic network sorts the warp's
+// keys by shuffles; `in` may equal `out` (every lane reads before any
+// writes).
+template <typename K>
+__global__ void __launch_bounds__(256) tiny_sort_kernel(const void* in_, void* out_,
+                                                        const TinySeg* segs, uint32_t nseg,
+                                                        uint32_t key_kind, uint32_t desc) {
+  const uint32_t w = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (w >= nseg) return;  // whole warps leave together
+  const uint32_t lane = threadIdx.x & 31;
+  const TinySeg sg = segs[w];
+  const OrderXform<K> kx(key_kind, desc != 0);
+  const K* in = static_cast<const K*>(in_) + sg.start;
+  K x = lane < sg.len ? kx.fwd(in[lane]) : ~K(0);
+#pragma unroll
+  for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const K y = __shfl_xor_sync(0xFFFFFFFFu, x, j);
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      x = keep_min ? (y < x ? y : x) : (y < x ? x : y);
+    }
+  }
+  if (lane < sg.len) static_cast<K*>(out_)[sg.start + lane] = kx.inv(x);
+}
 
 struct GroupSortParams {
   const void* in;
@@ -247,11 +287,13 @@ struct gs_seg_plan {
   bool desc = false;
   uint64_t n = 0;
   uint32_t ngroups = 0;
+  uint32_t ntiny = 0;
   uint32_t nlarge = 0;
   uint32_t large_tiles = 0;
   uint32_t tile = 0;
   int shape = 0;
   gs::SegGroup* d_groups = nullptr;
+  gs::TinySeg* d_tiny = nullptr;
   uint32_t* d_starts_rel = nullptr;
   uint32_t* d_tile_start = nullptr;
   uint64_t* d_range = nullptr;
@@ -273,13 +315,23 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
   pl->tile = radix_shape_tile(key_bytes, 0, shape);
   if (off[0] != 0 || off[nseg] != n) return "offsets must start at 0 and end at n";
   std::vector<SegGroup> groups;
+  std::vector<TinySeg> tiny;
   std::vector<uint32_t> rel;
   std::vector<uint32_t> tile_start;
   std::vector<uint64_t> range;
   SegGroup cur{};
+  uint32_t cur_max = 0;  // longest segment of the open group
   bool open = false;
   auto close = [&]() {
-    if (open && cur.count > 0) {
+    if (open && cur.count > 0 && cur_max <= TINY_KEYS) {
+      // Only tiny segments: one warp each instead of a group sort.
+      rel.push_back(cur.count);
+      for (uint32_t i = 0; i < cur.nsegs; ++i) {
+        const uint32_t a = rel[cur.first_seg + i], z = rel[cur.first_seg + i + 1];
+        tiny.push_back(TinySeg{cur.start + a, z - a, 0});
+      }
+      rel.resize(cur.first_seg);
+    } else if (open && cur.count > 0) {
       rel.push_back(cur.count);  // end of the last segment
       groups.push_back(cur);
     } else if (open) {
@@ -305,16 +357,19 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
         cur.start + cur.count != b) {
       close();
       cur = SegGroup{b, 0, uint32_t(rel.size()), 0, 0};
+      cur_max = 0;
       open = true;
     }
     rel.push_back(cur.count);
     cur.count += uint32_t(len);
     cur.nsegs += 1;
+    cur_max = std::max(cur_max, uint32_t(len));
   }
   close();
   if (tiles > 0xFFFFFFF0ull) return "too many tiles";
   tile_start.push_back(uint32_t(tiles));
   pl->ngroups = uint32_t(groups.size());
+  pl->ntiny = uint32_t(tiny.size());
   pl->nlarge = uint32_t(range.size() / 2);
   pl->large_tiles = uint32_t(tiles);
   auto up = [](void** dst, const void* src, size_t bytes) -> bool {
@@ -323,6 +378,7 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
   };
   bool ok = up(reinterpret_cast<void**>(&pl->d_groups), groups.data(), groups.size() * sizeof(SegGroup)) &&
+            up(reinterpret_cast<void**>(&pl->d_tiny), tiny.data(), tiny.size() * sizeof(TinySeg)) &&
             up(reinterpret_cast<void**>(&pl->d_starts_rel), rel.data(), rel.size() * 4) &&
             up(reinterpret_cast<void**>(&pl->d_tile_start), tile_start.data(), tile_start.size() * 4) &&
             up(reinterpret_cast<void**>(&pl->d_range), range.data(), range.size() * 8);
@@ -338,8 +394,8 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
 }
 
 void seg_plan_free(gs_seg_plan* pl) {
-  void* ps[] = {pl->d_groups, pl->d_starts_rel, pl->d_tile_start, pl->d_range, pl->d_hist,
-                pl->d_work};
+  void* ps[] = {pl->d_groups, pl->d_tiny, pl->d_starts_rel, pl->d_tile_start, pl->d_range,
+                pl->d_hist, pl->d_work};
   for (void* p : ps)
     if (p) cudaFree(p);
   delete pl;
@@ -355,6 +411,12 @@ cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* al
                       uint64_t* status, uint32_t* gen_counter, uint32_t* err, uint32_t spin_limit,
                       const DeviceProps& props, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
+  if (pl->ntiny) {
+    tiny_sort_kernel<K><<<(pl->ntiny + 7) / 8, 256, 0, st>>>(in, out, pl->d_tiny, pl->ntiny,
+                                                            pl->kind, uint32_t(pl->desc));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   if (pl->ngroups) {
     GroupSortParams gp{in, out, pl->d_groups, pl->d_starts_rel, pl->kind, pl->desc};
     constexpr size_t dyn = group_sort_dyn_smem<K>();

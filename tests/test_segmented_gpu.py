@@ -20,6 +20,13 @@ def _layouts():
     yield "boundaries", np.cumsum([0, 4095, 4096, 4097, 6143, 6144, 6145, 8192, 1, 12289]
                                   ).astype(np.uint64)
     yield "loguniform", datagen.segment_offsets(2000, 16, 1 << 17, total=1 << 22, seed=9)
+    # groups made only of segments of <= 32 keys take the warp bitonic path
+    yield "all_tiny", np.concatenate([[0], np.cumsum(rng.integers(1, 33, 5000))]).astype(np.uint64)
+    runs = []
+    for r in range(60):
+        runs += list(rng.integers(1, 33, int(rng.integers(1, 300))))
+        runs.append(int(rng.integers(33, 9000)))
+    yield "tiny_runs", np.concatenate([[0], np.cumsum(runs)]).astype(np.uint64)
 
 
 @pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float32, np.uint64, np.int64,
