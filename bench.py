@@ -67,11 +67,11 @@ sys.path.insert(0, str(ROOT))
 
 B_ALG_PER_KEY_U32 = 36          # 4 * (2 * 4 + 1): histogram read + 4 passes
 PASS_BYTES_PER_KEY_U32 = 8      # one pass reads and writes each 4-byte key
-# DRAM bytes per key of one stable pass launch, from the ncu capture of a
-# 2^26-key sort (dram__bytes_read.sum + dram__bytes_write.sum = 493.3 MB per
-# launch, profiles/pass_kernel_u32_2e26_full.md); traffic is per key
+# DRAM bytes per key of one pass launch, from the ncu capture of a 2^26-key
+# sort (dram__bytes_read.sum + dram__bytes_write.sum = 493.6 MB per launch,
+# the mean of its four passes, profiles/pass_kernel_u32_2e26_full.md); traffic is per key
 # (streaming reads and writes), so it scales to 2^30 by the key count.
-PASS_TRAFFIC_PER_KEY_U32 = 493.3e6 / (1 << 26)
+PASS_TRAFFIC_PER_KEY_U32 = 493.6e6 / (1 << 26)
 METRIC = "sort throughput (Gkeys/s)"
 WORKLOAD = "single-array sort, 2^{} uint32 keys uniform over [0, 2^32), ascending"
 

@@ -20,6 +20,7 @@ enum KeyKind : uint32_t { KIND_UNSIGNED = 0, KIND_SIGNED = 1, KIND_FLOAT = 2 };
 enum ErrBits : uint32_t {
   ERR_LOOKBACK_TIMEOUT = 1u,
   ERR_SCATTER_RANGE = 2u,
+  ERR_PASS_KIND = 4u,  // an unstable-only pass kernel launched for a stable pass
   ERR_SMEM_ALIGN = 8u
 };
 
@@ -89,6 +90,20 @@ __device__ __forceinline__ uint64_t ld_stream(const uint64_t* p) {
   uint64_t v;
   asm("ld.global.cs.u64 %0, [%1];" : "=l"(v) : "l"(p));
   return v;
+}
+// Four consecutive 32-bit words; p is 16-byte aligned.
+__device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p) {
+  uint4 v;
+  asm("ld.global.cs.v4.u32 {%0, %1, %2, %3}, [%4];"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+  return v;
+}
+
+// Bulk prefetch of [p, p + bytes) into L2 (one instruction, one thread):
+// p 16-byte aligned, bytes a non-zero multiple of 16, the range inside the
+// allocation.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
 // Shared-memory address of a generic pointer (alignment checks).

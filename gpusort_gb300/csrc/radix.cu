@@ -121,16 +121,18 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   using Sh = PassShape<K, V, S>;
   using Cfg = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, Sh::RANK>;
   // The lowest digit's pass, when it runs, is the first one and ranks
-  // unstably (keys only): half-warp ranking gains nothing there and its
-  // larger offset table costs L1 capacity (2^30 u32: 3.05 vs 3.20 ms), so
-  // that launch takes the table variant of the same tile.
-  using Cfg0 = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, RANK_TABLE>;
-  static_assert(Cfg0::TILE == Cfg::TILE, "one tile layout for every pass of a sort");
+  // unstably in keys-only sorts. Those launch it with the unstable-only
+  // kernel of the same tile (2^30 u32 keys: 2.94 -> 2.65 ms against the
+  // table kernel's unstable branch; 2^29 u64 keys: 2.43 -> 2.19 ms).
+  constexpr bool HAS_V = !std::is_same<V, NoValue>::value;
+  using CfgU = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, RANK_UNSTABLE>;
+  static_assert(CfgU::TILE == Cfg::TILE, "one tile layout for every pass of a sort");
   cudaError_t e = cudaSuccess;
   auto kern = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK>;
-  auto kern0 = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, RANK_TABLE>;
+  auto kernu = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, HAS_V ? Sh::RANK : RANK_UNSTABLE>;
   e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
-  if (e == cudaSuccess) e = allow_dynamic_smem(reinterpret_cast<const void*>(kern0), Cfg0::DYN_SMEM);
+  if (e == cudaSuccess && !HAS_V)
+    e = allow_dynamic_smem(reinterpret_cast<const void*>(kernu), CfgU::DYN_SMEM);
   if (e != cudaSuccess) return e;
   const uint64_t tiles = sj != nullptr ? sj->total_tiles : (job.n + Cfg::TILE - 1) / Cfg::TILE;
   PassParams pa{};
@@ -161,13 +163,17 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   }
   if (tiles == 0) return cudaSuccess;
   (void)gen;
+  // Each CTA prefetches the tile one wave of resident CTAs ahead into L2,
+  // the tile a CTA claims about when this one finishes (2^30 u32 keys:
+  // passes 3.54 -> 3.48 ms; 2^29 u64 keys: 2.77 -> 2.58 ms; two waves
+  // ahead gained less).
+  pa.prefetch_tiles = sj == nullptr ? uint32_t(props.num_sms * Sh::MINB) : 0u;
   const uint32_t qlo = job.digit_hi ? job.digit_lo : 0u;
   const uint32_t qhi = job.digit_hi ? job.digit_hi : digits;
-  const bool table_first = Sh::RANK == RANK_HALF && pa.first_unstable;
   for (uint32_t q = qlo; q < qhi; ++q) {
     pa.pass = q;
-    if (q == qlo && table_first)
-      kern0<<<unsigned(tiles), Sh::THREADS, Cfg0::DYN_SMEM, stream>>>(pa);
+    if (q == qlo && !HAS_V && pa.first_unstable)
+      kernu<<<unsigned(tiles), Sh::THREADS, CfgU::DYN_SMEM, stream>>>(pa);
     else
       kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM, stream>>>(pa);
     e = cudaGetLastError();
@@ -346,7 +352,8 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   // 16 (32-bit keys) or 12 (64-bit keys) items per thread leave registers
   // for the packed bucket ids.
   using Sh = Shape<512, sizeof(K) == 4 ? 16 : 12, 2>;
-  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::RANK>;
+  // The bucket scatter ranks unstably: the unstable-only kernel.
+  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS, RANK_UNSTABLE>;
   PlanParams pp{};
   pp.work = job.work;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
@@ -356,7 +363,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.digit_lo = 0;
   pp.digit_hi = 1;
   plan_kernel<<<1, 256, 0, st>>>(pp);
-  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK, true>;
+  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, RANK_UNSTABLE, true>;
   cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM_BUCKET);
   if (e != cudaSuccess) return e;
   PassParams pa{};
@@ -375,6 +382,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pa.pass = 0;
   pa.splitters = splitters;
   pa.nsplit = nsplit;
+  pa.prefetch_tiles = uint32_t(props.num_sms * Sh::MINB);
   const uint64_t tiles = (job.n + Cfg::TILE - 1) / Cfg::TILE;
   kern<<<unsigned(tiles), Sh::THREADS, Cfg::DYN_SMEM_BUCKET, st>>>(pa);
   return cudaGetLastError();

@@ -89,6 +89,12 @@ upsweep_kernel(UpsweepParams p) {
   const uint64_t n = p.n;
   const uint64_t chunk = uint64_t(THREADS) * UNROLL;
   K* const copy_k = static_cast<K*>(p.copy_keys);
+  // Keys only: interior chunks are read as 16-byte vectors when the
+  // buffers are 16-byte aligned (2^30 u32 keys: 1.00 -> 0.82 ms).
+  constexpr int KPV = int(16 / sizeof(K));  // keys per vector
+  constexpr bool VEC = !HAS_V && UNROLL % KPV == 0;
+  const bool vec = VEC && (reinterpret_cast<uintptr_t>(keys) & 15u) == 0 &&
+                   (reinterpret_cast<uintptr_t>(copy_k) & 15u) == 0;
   V* copy_v = nullptr;
   if constexpr (HAS_V) copy_v = static_cast<V*>(p.copy_vals);
   // Pair sorts: -0.0 counts as +0.0 (see pass_kernel).
@@ -150,6 +156,44 @@ upsweep_kernel(UpsweepParams p) {
        base += uint64_t(gridDim.x) * chunk) {
     K k[UNROLL];
     bool valid[UNROLL];
+    if (VEC && vec && base + chunk <= n) {
+      // Interior chunk, keys only: thread t's items are the keys of 16-byte
+      // vectors t, t + THREADS, ... (the order of a histogram's counts does
+      // not matter).
+      const uint32_t* kb = reinterpret_cast<const uint32_t*>(keys + base);
+#pragma unroll
+      for (int u = 0; u < UNROLL / KPV; ++u) {
+        const uint4 q = ld_stream_v4(kb + 4 * (u * THREADS + threadIdx.x));
+        if constexpr (KPV == 4) {
+          k[4 * u] = K(q.x);
+          k[4 * u + 1] = K(q.y);
+          k[4 * u + 2] = K(q.z);
+          k[4 * u + 3] = K(q.w);
+        } else {
+          k[2 * u] = K(q.x) | (K(q.y) << 32);
+          k[2 * u + 1] = K(q.z) | (K(q.w) << 32);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) valid[u] = true;
+      if (copy_k) {
+        uint32_t* cb = reinterpret_cast<uint32_t*>(copy_k + base);
+#pragma unroll
+        for (int u = 0; u < UNROLL / KPV; ++u) {
+          uint4 q;
+          if constexpr (KPV == 4) {
+            q = make_uint4(uint32_t(k[4 * u]), uint32_t(k[4 * u + 1]), uint32_t(k[4 * u + 2]),
+                           uint32_t(k[4 * u + 3]));
+          } else {
+            q = make_uint4(uint32_t(k[2 * u]), uint32_t(k[2 * u] >> 32), uint32_t(k[2 * u + 1]),
+                           uint32_t(k[2 * u + 1] >> 32));
+          }
+          *reinterpret_cast<uint4*>(cb + 4 * (u * THREADS + threadIdx.x)) = q;
+        }
+      }
+      count(k, valid);
+      continue;
+    }
     if (base + chunk <= n) {  // interior chunk: no bounds checks
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
@@ -203,7 +247,11 @@ upsweep_kernel(UpsweepParams p) {
 //                bound the pass. Eight warp ballots per row instead of the
 //                peer table halve the shared-memory wavefronts but triple
 //                the ALU instructions and made the pass ALU-bound (4.51 ms).
-enum RankMode : int { RANK_TABLE = 0, RANK_HALF = 2 };
+//   RANK_UNSTABLE - the keys-only lowest-digit pass, which always ranks
+//                unstably (one shared atomic per element): without the
+//                stable rankings' code and tables the kernel keeps its
+//                registers and leaves more of the SM's L1 as cache.
+enum RankMode : int { RANK_TABLE = 0, RANK_UNSTABLE = 1, RANK_HALF = 2 };
 
 template <typename K, typename V, int THREADS, int ITEMS, int RANK = RANK_TABLE>
 struct PassConfig {
@@ -223,15 +271,16 @@ struct PassConfig {
   // apart in the tile.
   static constexpr int STRIDE = RANK == RANK_HALF ? 16 : 32;
   static constexpr size_t TAB_BYTES =
-      RANK == RANK_TABLE ? size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t)
-                         : ((size_t(WARPS) * (RADIX + 1) * 2 * sizeof(uint32_t) + 15) & ~size_t(15));
+      RANK == RANK_UNSTABLE ? size_t(RADIX) * sizeof(uint32_t)
+      : RANK == RANK_TABLE  ? size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t)
+                            : ((size_t(WARPS) * (RADIX + 1) * 2 * sizeof(uint32_t) + 15) & ~size_t(15));
   static_assert(TAB_BYTES % 16 == 0, "the table is cleared in 16-byte units");
   static constexpr size_t STAGE_BYTES = SMEM_KEYS + SMEM_VALS;
   static constexpr size_t UNION_BYTES = ((STAGE_BYTES > TAB_BYTES ? STAGE_BYTES : TAB_BYTES) + 15) & ~size_t(15);
   // Per warp and digit: a 16-bit tile offset, or (RANK_HALF) two, one per
   // half, in one 32-bit word.
   using OffT = typename std::conditional<RANK == RANK_HALF, uint32_t, uint16_t>::type;
-  static constexpr size_t OFF_BYTES = size_t(WARPS) * RADIX * sizeof(OffT);
+  static constexpr size_t OFF_BYTES = size_t(RANK == RANK_UNSTABLE ? 1 : WARPS) * RADIX * sizeof(OffT);
   static constexpr size_t DYN_SMEM = UNION_BYTES + OFF_BYTES;
   // BUCKET mode also stages each element's bucket (one byte) for the scatter.
   static constexpr size_t DYN_SMEM_BUCKET = DYN_SMEM + size_t(TILE);
@@ -318,6 +367,10 @@ pass_kernel(PassParams p) {
   SortPlan& plan = p.work->plan;
   const uint32_t j = plan.exec_index[p.pass];
   if (j == PASS_SKIPPED) return;
+  if (RANK == RANK_UNSTABLE && !(j == 0 && p.first_unstable && !plan.first_stable)) {
+    if (threadIdx.x == 0) atomicOr(p.err, ERR_PASS_KIND);
+    return;
+  }
   const uint32_t m = plan.m_exec;
   const uint32_t gen = (plan.gen_base + p.pass + 1) & GEN_MASK;  // this pass's look-back tag
   const bool first = (j == 0);
@@ -343,7 +396,7 @@ pass_kernel(PassParams p) {
   // requested order leaves no ties to preserve (keys only, or pairs ordered
   // by value too): equal digits there are either equal in every later digit
   // (identical elements) or separated by a later, stable pass.
-  const bool unstable = first && p.first_unstable && !plan.first_stable;
+  const bool unstable = RANK == RANK_UNSTABLE || (first && p.first_unstable && !plan.first_stable);
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -357,15 +410,28 @@ pass_kernel(PassParams p) {
   // Tiles are claimed in launch order, so a tile only ever waits on tiles
   // held by CTAs that are already running.
   if (tid == 0) {
-    s_tile = atomicAdd(&plan.tile_counter[p.pass], 1u);
+    const uint32_t t = atomicAdd(&plan.tile_counter[p.pass], 1u);
+    s_tile = t;
     s_bad = 0;
+    if (p.prefetch_tiles != 0 && p.seg_tile_start == nullptr && !reverse) {
+      const uint64_t b = (uint64_t(t) + p.prefetch_tiles) * TILE;
+      if (b < n) {
+        const uint64_t c = n - b < uint64_t(TILE) ? n - b : uint64_t(TILE);
+        auto pf = [](const void* a, uint64_t bytes) {
+          bytes &= ~uint64_t(15);
+          if ((reinterpret_cast<uintptr_t>(a) & 15u) == 0 && bytes != 0) prefetch_l2_bulk(a, uint32_t(bytes));
+        };
+        pf(src_k + b, c * sizeof(K));
+        if constexpr (HAS_V) pf(src_v + b, c * sizeof(VS));
+      }
+    }
   }
   if ((smem_addr(s_dyn) & 15u) == 0) {
     uint4* z = reinterpret_cast<uint4*>(s_dyn);
     // The unstable ranking uses only the first RADIX words. (Only the
     // keys-only table kernels, which run the lowest digit's unstable pass,
     // skip the rest: the same branch costs the other kernels registers.)
-    if (!HAS_V && RANK == RANK_TABLE && unstable) {
+    if (RANK == RANK_UNSTABLE || (!HAS_V && RANK == RANK_TABLE && unstable)) {
       if (tid < RADIX / 4) z[tid] = make_uint4(0, 0, 0, 0);
     } else {
       constexpr int Z = int(Cfg::TAB_BYTES / 16);
@@ -486,7 +552,14 @@ pass_kernel(PassParams p) {
     auto get_rank = [&](int i) -> uint32_t { return (rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu; };
 
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_dyn);
-    if (unstable) {
+    if constexpr (RANK == RANK_UNSTABLE) {
+      // The tile's digit counts; each element takes its place in the
+      // reorder below, by one more atomic on the digit's running offset.
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (in_tile(wloc + STRIDE * i)) atomicAdd(&s_cnt[digit_at(i)], 1u);
+      }
+    } else if (unstable) {
       // One shared atomic per element: its rank among the tile's elements of
       // the same digit, in no particular order.
 #pragma unroll
@@ -518,7 +591,7 @@ pass_kernel(PassParams p) {
         if (below == 0) *e = (base + __popc(peers)) << 16;
         __syncwarp();
       }
-    } else {
+    } else if constexpr (RANK == RANK_TABLE) {
       // Stable warp ranking: each lane sets its bit in the digit's peer mask,
       // reads back the mask and the digit's running count; the group's lowest
       // lane advances the count and clears the mask.
@@ -583,30 +656,24 @@ pass_kernel(PassParams p) {
     const uint32_t tile_excl = block_excl_scan_256(count, s_tmp, s_excl);
 
     // Per warp and digit: where the ranker's elements of the digit start in
-    // the reordered tile. With more than 256 threads the upper ones write
-    // these while the first 256 run the look-back below.
-    auto write_offsets = [&](uint32_t d) {
-      uint32_t run = s_excl[d];
-      if (unstable) {
-        s_offd[0][d] = OffT(RANK == RANK_HALF ? (run | (run << 16)) : run);
-        return;
-      }
+    // the reordered tile.
+    // (The unstable-only kernel places elements by running offsets instead.)
+    if constexpr (RANK != RANK_UNSTABLE) {
+      if (tid < RADIX) {
+        const uint32_t d = uint32_t(tid);
+        uint32_t run = tile_excl;
+        if (unstable) {
+          s_offd[0][d] = OffT(RANK == RANK_HALF ? (run | (run << 16)) : run);
+        } else {
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) {
-        uint32_t c0, c1;
-        ranker_counts(w, d, c0, c1);
-        s_offd[w][d] = OffT(RANK == RANK_HALF ? (run | ((run + c0) << 16)) : run);
-        run += c0 + c1;
+          for (int w = 0; w < WARPS; ++w) {
+            uint32_t c0, c1;
+            ranker_counts(w, d, c0, c1);
+            s_offd[w][d] = OffT(RANK == RANK_HALF ? (run | ((run + c0) << 16)) : run);
+            run += c0 + c1;
+          }
+        }
       }
-    };
-    if constexpr (THREADS >= 2 * RADIX || (THREADS > RADIX && RANK == RANK_HALF)) {
-      // Threads past the first 256 take the digits in turn (two each with
-      // 384 threads: 2^30 u32 keys 14.75 -> 14.59 ms; the pair kernels,
-      // with cheaper 16-bit offsets, spilled more and kept the first 256).
-      for (int d = tid - RADIX; d >= 0 && d < RADIX; d += THREADS - RADIX)
-        write_offsets(uint32_t(d));
-    } else {
-      if (tid < RADIX) write_offsets(uint32_t(tid));
     }
 
     // Decoupled look-back over preceding tiles, LB_WIN words per round,
@@ -614,6 +681,7 @@ pass_kernel(PassParams p) {
     // is pending, one word is polled per round after a short sleep, so
     // waiting warps leave issue slots and L1 bandwidth to the tiles they
     // wait for.
+    auto lookback = [&]() {
     uint32_t prefix = 0;
     if (tid < RADIX) {
       if (tile > first_unit) {
@@ -667,24 +735,34 @@ pass_kernel(PassParams p) {
         atomicOr(p.err, ERR_SCATTER_RANGE);
       }
     }
-    __syncthreads();
+    };
 
     // Reorder the tile in shared memory by digit (keys in transformed form).
     K* s_keys = reinterpret_cast<K*>(s_dyn);
     VS* s_vals = reinterpret_cast<VS*>(s_dyn + Cfg::SMEM_KEYS);
     uint8_t* s_bdig = s_dyn + Cfg::DYN_SMEM;  // BUCKET mode only
-    const OffT* s_off = s_offd[unstable ? 0 : warp];
-    const uint32_t hsh = RANK == RANK_HALF ? 16u * (uint32_t(lane) >> 4) : 0u;
+    auto reorder = [&]() {
+      const OffT* s_off = s_offd[unstable ? 0 : warp];
+      const uint32_t hsh = RANK == RANK_HALF ? 16u * (uint32_t(lane) >> 4) : 0u;
 #pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      if (in_tile(wloc + STRIDE * i)) {
-        const uint32_t d = digit_at(i);
-        const uint32_t pos = ((uint32_t(s_off[d]) >> hsh) & 0xFFFFu) + get_rank(i);
-        s_keys[pos] = keys[i];
-        if constexpr (HAS_V) s_vals[pos] = vals[i];
-        if constexpr (BUCKET) s_bdig[pos] = uint8_t(d);
+      for (int i = 0; i < ITEMS; ++i) {
+        if (in_tile(wloc + STRIDE * i)) {
+          const uint32_t d = digit_at(i);
+          uint32_t pos;
+          if constexpr (RANK == RANK_UNSTABLE) pos = atomicAdd(&s_excl[d], 1u);
+          else pos = ((uint32_t(s_off[d]) >> hsh) & 0xFFFFu) + get_rank(i);
+          s_keys[pos] = keys[i];
+          if constexpr (HAS_V) s_vals[pos] = vals[i];
+          if constexpr (BUCKET) s_bdig[pos] = uint8_t(d);
+        }
       }
-    }
+    };
+    // The reorder needs only the tile's own offsets, so it runs before the
+    // look-back, which then finds more of the preceding tiles done (2^30 u32
+    // keys: stable passes 3.58 -> 3.54 ms against the look-back first).
+    __syncthreads();
+    reorder();
+    lookback();
     __syncthreads();
 
     // Scatter: consecutive tile positions of one digit go to consecutive

@@ -92,6 +92,9 @@ struct PassParams {
   // among nsplit + 1 <= RADIX buckets; splitters are sorted order bits.
   const void* splitters;
   uint32_t nsplit;
+  // Unsegmented forward passes: tile t's CTA prefetches tile t +
+  // prefetch_tiles of its source into L2 (0: none).
+  uint32_t prefetch_tiles;
 };
 
 }  // namespace gs
