@@ -90,8 +90,10 @@ constexpr int UPSWEEP_PER_SM = 3;
 //    threads and keep 512.
 //  - Shape 1: 256 threads, 4 CTAs per SM, for small sorts.
 //  - Shape 2: 512 threads, 2 CTAs per SM (the previous default).
-// Keys rank by half-warps (2^30 u32: stable passes 3.97 vs 4.30 ms with the
-// 64-bit table), pairs by the table (2^29 u64 + u32: 56.0 vs 56.6 ms).
+// Keys and pairs rank by half-warps: 2^30 u32 keys, stable passes 3.97 vs
+// 4.30 ms with the 64-bit table; 2^29 pairs (same 384-thread tile, table vs
+// half-warp): u64 Zipf(1.1) + u32 index, stable, 33.6 -> 30.9 ms (skewed
+// digits), u64 + u32 uniform 50.0 -> 49.8 ms, u32 + u32 24.7 -> 24.3 ms.
 template <int T, int I, int B, int R = RANK_TABLE> struct Shape {
   static constexpr int THREADS = T, ITEMS = I, MINB = B, RANK = R;
 };
@@ -102,14 +104,14 @@ template <> struct PassShape<uint32_t, NoValue, 2> : Shape<512, 24, 2, RANK_HALF
 template <> struct PassShape<uint64_t, NoValue, 0> : Shape<384, 14, 3, RANK_HALF> {};
 template <> struct PassShape<uint64_t, NoValue, 1> : Shape<256, 12, 4> {};
 template <> struct PassShape<uint64_t, NoValue, 2> : Shape<512, 14, 2, RANK_HALF> {};
-template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<384, 14, 3> {};
+template <> struct PassShape<uint32_t, uint32_t, 0> : Shape<384, 14, 3, RANK_HALF> {};
 template <> struct PassShape<uint32_t, uint32_t, 1> : Shape<256, 12, 4> {};
 template <> struct PassShape<uint32_t, uint32_t, 2> : Shape<512, 14, 2> {};
 template <> struct PassShape<uint64_t, uint64_t, 0> : Shape<512, 9, 2> {};
 template <> struct PassShape<uint64_t, uint64_t, 2> : Shape<512, 9, 2, RANK_HALF> {};
 template <typename K, typename V, int S>
 struct PassShape : Shape<(S == 0 ? 384 : S == 1 ? 256 : 512), (S == 1 ? 6 : 10),
-                         (S == 0 ? 3 : S == 1 ? 4 : 2), RANK_TABLE> {};
+                         (S == 0 ? 3 : S == 1 ? 4 : 2), (S == 0 ? RANK_HALF : RANK_TABLE)> {};
 constexpr int NUM_SHAPES = 3;
 constexpr uint32_t MIN_TILE = 1024;  // no shape has a smaller tile (smallest: 256 x 6)
 
