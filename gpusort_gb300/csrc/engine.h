@@ -94,6 +94,8 @@ size_t radix_status_words(uint64_t n, int key_bytes, int val_bytes);
 size_t sort_work_bytes();
 
 // Large segments of a batched sort, for the segmented form of the passes.
+struct SegTile;  // radix_types.cuh
+
 struct SegJob {
   const uint32_t* tile_start;  // nseg + 1 first-tile indexes
   const uint64_t* range;       // nseg (begin, end) element pairs
@@ -101,6 +103,7 @@ struct SegJob {
   uint32_t nseg;
   uint32_t digits;
   uint32_t total_tiles;
+  const SegTile* tiles;        // total_tiles descriptors
 };
 uint32_t radix_shape_tile(int key_bytes, int val_bytes, int shape);
 int radix_segmented_shape(int key_bytes, uint64_t n, uint32_t nseg);

@@ -130,8 +130,13 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   using CfgU = PassConfig<K, V, Sh::THREADS, Sh::ITEMS, RANK_UNSTABLE>;
   static_assert(CfgU::TILE == Cfg::TILE, "one tile layout for every pass of a sort");
   cudaError_t e = cudaSuccess;
-  auto kern = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK>;
-  auto kernu = pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, HAS_V ? Sh::RANK : RANK_UNSTABLE>;
+  // Segmented sorts (keys only) run the SEG form of the same kernels.
+  const bool seg = sj != nullptr;
+  auto kern = seg ? pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK, false, !HAS_V>
+                  : pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK>;
+  auto kernu = seg ? pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, HAS_V ? Sh::RANK : RANK_UNSTABLE,
+                                 false, !HAS_V>
+                   : pass_kernel<K, V, Sh::THREADS, Sh::ITEMS, Sh::MINB, HAS_V ? Sh::RANK : RANK_UNSTABLE>;
   e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM);
   if (e == cudaSuccess && !HAS_V)
     e = allow_dynamic_smem(reinterpret_cast<const void*>(kernu), CfgU::DYN_SMEM);
@@ -157,7 +162,9 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   pa.work = job.work;
   pa.err = job.err;
   if (sj != nullptr) {
+    if (HAS_V || sj->tiles == nullptr) return cudaErrorInvalidValue;
     pa.seg_tile_start = sj->tile_start;
+    pa.seg_tiles = sj->tiles;
     pa.seg_range = sj->range;
     pa.seg_binbase = sj->binbase;
     pa.nseg = sj->nseg;
@@ -169,7 +176,7 @@ cudaError_t launch_passes(const RadixJob& job, const SegJob* sj, uint32_t digits
   // the tile a CTA claims about when this one finishes (2^30 u32 keys:
   // passes 3.54 -> 3.48 ms; 2^29 u64 keys: 2.77 -> 2.58 ms; two waves
   // ahead gained less).
-  pa.prefetch_tiles = sj == nullptr ? uint32_t(props.num_sms * Sh::MINB) : 0u;
+  pa.prefetch_tiles = uint32_t(props.num_sms * Sh::MINB);
   const uint32_t qlo = job.digit_hi ? job.digit_lo : 0u;
   const uint32_t qhi = job.digit_hi ? job.digit_hi : digits;
   for (uint32_t q = qlo; q < qhi; ++q) {

@@ -327,7 +327,7 @@ __device__ __forceinline__ uint32_t tree_bucket(const K* tree, uint32_t levels, 
 // runs transforms them on load, the last one restores raw bits on store.
 // Values stay raw and are transformed only to extract a value digit.
 template <typename K, typename V, int THREADS, int ITEMS, int MIN_BLOCKS, int RANK = RANK_TABLE,
-          bool BUCKET = false>
+          bool BUCKET = false, bool SEG = false>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 pass_kernel(PassParams p) {
   using Cfg = PassConfig<K, V, THREADS, ITEMS, RANK>;
@@ -360,7 +360,6 @@ pass_kernel(PassParams p) {
   __shared__ uint32_t s_excl[RADIX];  // the tile's exclusive digit offsets
   __shared__ uint32_t s_tmp[8];
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_seg;
   __shared__ uint32_t s_bad;  // a digit's destination range leaves the output
   __shared__ K s_split[BUCKET ? RADIX : 1];  // bucket mode: splitter search tree
 
@@ -409,22 +408,26 @@ pass_kernel(PassParams p) {
 
   // Tiles are claimed in launch order, so a tile only ever waits on tiles
   // held by CTAs that are already running.
+  // L2 prefetch of the elements prefetch_tiles tiles further on, which a
+  // CTA claims about when this one finishes (segmented sorts: the same
+  // distance in elements, a hint that may cross into later segments).
+  auto prefetch_from = [&](uint64_t b) {
+    if (b < n) {
+      const uint64_t c = n - b < uint64_t(TILE) ? n - b : uint64_t(TILE);
+      auto pf = [](const void* a, uint64_t bytes) {
+        bytes &= ~uint64_t(15);
+        if ((reinterpret_cast<uintptr_t>(a) & 15u) == 0 && bytes != 0) prefetch_l2_bulk(a, uint32_t(bytes));
+      };
+      pf(src_k + b, c * sizeof(K));
+      if constexpr (HAS_V) pf(src_v + b, c * sizeof(VS));
+    }
+  };
   if (tid == 0) {
     const uint32_t t = atomicAdd(&plan.tile_counter[p.pass], 1u);
     s_tile = t;
     s_bad = 0;
-    if (p.prefetch_tiles != 0 && p.seg_tile_start == nullptr && !reverse) {
-      const uint64_t b = (uint64_t(t) + p.prefetch_tiles) * TILE;
-      if (b < n) {
-        const uint64_t c = n - b < uint64_t(TILE) ? n - b : uint64_t(TILE);
-        auto pf = [](const void* a, uint64_t bytes) {
-          bytes &= ~uint64_t(15);
-          if ((reinterpret_cast<uintptr_t>(a) & 15u) == 0 && bytes != 0) prefetch_l2_bulk(a, uint32_t(bytes));
-        };
-        pf(src_k + b, c * sizeof(K));
-        if constexpr (HAS_V) pf(src_v + b, c * sizeof(VS));
-      }
-    }
+    if (!SEG && p.prefetch_tiles != 0 && !reverse)
+      prefetch_from((uint64_t(t) + p.prefetch_tiles) * TILE);
   }
   if ((smem_addr(s_dyn) & 15u) == 0) {
     uint4* z = reinterpret_cast<uint4*>(s_dyn);
@@ -448,24 +451,22 @@ pass_kernel(PassParams p) {
   // tile, where the segment's look-back chain starts.
   uint32_t seg = 0, first_unit = 0;
   uint64_t e0 = 0, e1 = n;
-  if (p.seg_tile_start != nullptr) {
-    if (tid == 0) {
-      uint32_t lo = 0, hi = p.nseg;  // last s with seg_tile_start[s] <= tile
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (p.seg_tile_start[mid] <= tile) lo = mid; else hi = mid;
-      }
-      s_seg = lo;
-    }
-    __syncthreads();
-    seg = s_seg;
+  uint64_t tile_base;
+  uint32_t tile_n;
+  if constexpr (SEG) {
+    const SegTile d = p.seg_tiles[tile];
+    seg = d.seg;
+    tile_base = d.base;
+    tile_n = d.n;
     first_unit = p.seg_tile_start[seg];
     e0 = p.seg_range[2 * seg];
     e1 = p.seg_range[2 * seg + 1];
+    if (tid == 0 && p.prefetch_tiles != 0 && !reverse)
+      prefetch_from(tile_base + uint64_t(p.prefetch_tiles) * TILE);
+  } else {
+    tile_base = uint64_t(tile) * TILE;
+    tile_n = tile_base >= n ? 0u : uint32_t(n - tile_base < uint64_t(TILE) ? n - tile_base : uint64_t(TILE));
   }
-  const uint64_t tile_base = e0 + uint64_t(tile - first_unit) * TILE;
-  const uint32_t tile_n =
-      tile_base >= e1 ? 0u : uint32_t(e1 - tile_base < uint64_t(TILE) ? e1 - tile_base : uint64_t(TILE));
   // Tile index of item 0; item i is STRIDE further. RANK_HALF: lanes 0-15
   // and 16-31 of a warp hold two consecutive runs of 16 * ITEMS elements.
   const uint32_t ranker = RANK == RANK_HALF ? uint32_t(2 * warp + (lane >> 4)) : uint32_t(warp);

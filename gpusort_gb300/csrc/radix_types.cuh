@@ -58,6 +58,14 @@ struct PlanParams {
   uint32_t drop_reverse;
 };
 
+// One tile of a segmented pass: its first element, element count and
+// segment (built with the plan, so a tile finds its place with one load).
+struct SegTile {
+  uint64_t base;
+  uint32_t n;
+  uint32_t seg;
+};
+
 struct PassParams {
   const void* keys_in;
   void* keys_out;
@@ -84,6 +92,7 @@ struct PassParams {
   // first tile starts its own look-back chain.
   const uint32_t* seg_tile_start;
   const uint64_t* seg_range;
+  const SegTile* seg_tiles;  // per tile
   const uint32_t* seg_binbase;
   uint32_t nseg;
   uint32_t seg_digits;

@@ -216,38 +216,108 @@ struct SegHistParams {
   uint32_t* hist;       // [nseg][digits][RADIX]
 };
 
+// Each CTA takes a contiguous run of tiles, so consecutive tiles mostly
+// belong to one segment: the CTA counts into shared memory and adds its
+// counts to the segment's histogram only when the segment changes, and at
+// the end. Every bin has SEG_HIST_COLS columns, lane l counting into column
+// l mod SEG_HIST_COLS, so a warp's atomics to random bins spread over more
+// banks. (100,000 segments, ~2^30 u32 keys: one counter per bin, tiles
+// strided over the grid and a flush per tile took 2.3 ms.)
+constexpr int SEG_HIST_THREADS = 256;
+constexpr int SEG_HIST_UNROLL = 3;  // 16-byte vectors in flight per thread
+template <typename K> __host__ __device__ constexpr int seg_hist_cols() { return sizeof(K) == 4 ? 8 : 4; }
+template <typename K> constexpr size_t seg_hist_smem() {
+  return size_t(Bits<K>::DIGITS) * RADIX * seg_hist_cols<K>() * sizeof(uint32_t);
+}
+
 template <typename K>
-__global__ void __launch_bounds__(256) seg_hist_kernel(SegHistParams p) {
+__global__ void __launch_bounds__(SEG_HIST_THREADS) seg_hist_kernel(SegHistParams p) {
   constexpr int KD = Bits<K>::DIGITS;
-  __shared__ uint32_t s_h[KD * RADIX];
-  __shared__ uint32_t s_seg;
+  constexpr uint32_t NC = seg_hist_cols<K>();
+  constexpr uint32_t WORDS = KD * RADIX * NC;
+  extern __shared__ __align__(16) uint32_t s_h[];  // [digit][bin][column]
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const K* keys = static_cast<const K*>(p.keys);
-  for (uint32_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-    for (int i = threadIdx.x; i < KD * RADIX; i += blockDim.x) s_h[i] = 0;
-    if (threadIdx.x == 0) {
-      uint32_t lo = 0, hi = p.nseg;
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (p.seg_tile_start[mid] <= t) lo = mid; else hi = mid;
-      }
-      s_seg = lo;
-    }
-    __syncthreads();
-    const uint32_t s = s_seg;
-    const uint64_t b = p.seg_range[2 * s] + uint64_t(t - p.seg_tile_start[s]) * p.tile;
-    const uint64_t e = min(b + p.tile, p.seg_range[2 * s + 1]);
-    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-      const K v = kx.fwd(keys[i]);
+  const uint32_t tid = threadIdx.x;
+  uint32_t* const hk = s_h + (tid & (NC - 1));
+  constexpr uint32_t KPV = 16 / sizeof(K);  // keys per 16-byte vector
+  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
+  auto count = [&](K v) {
 #pragma unroll
-      for (int d = 0; d < KD; ++d) atomicAdd(&s_h[d * RADIX + (uint32_t(v >> (8 * d)) & 255)], 1u);
+    for (int d = 0; d < KD; ++d) atomicAdd(hk + (d * RADIX + (uint32_t(v >> (8 * d)) & 255u)) * NC, 1u);
+  };
+  const uint32_t per = (p.total_tiles + gridDim.x - 1) / gridDim.x;
+  const uint32_t t0 = blockIdx.x * per;
+  const uint32_t t1 = min(t0 + per, p.total_tiles);
+  if (t0 >= t1) return;
+  for (uint32_t i = tid; i < WORDS; i += SEG_HIST_THREADS) s_h[i] = 0;
+  // The segment of tile t0: the last s with seg_tile_start[s] <= t0 (every
+  // thread finds the same one).
+  uint32_t seg = 0;
+  {
+    uint32_t lo = 0, hi = p.nseg;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (p.seg_tile_start[mid] <= t0) lo = mid; else hi = mid;
     }
+    seg = lo;
+  }
+  __syncthreads();
+  auto flush = [&](uint32_t s) {
     __syncthreads();
     uint32_t* g = p.hist + size_t(s) * KD * RADIX;
-    for (int i = threadIdx.x; i < KD * RADIX; i += blockDim.x)
-      if (s_h[i]) atomicAdd(&g[i], s_h[i]);
+    for (uint32_t i = tid; i < uint32_t(KD * RADIX); i += SEG_HIST_THREADS) {
+      uint32_t c = 0;
+#pragma unroll
+      for (uint32_t j = 0; j < NC; ++j) {
+        const uint32_t w = i * NC + ((j + i) & (NC - 1));
+        c += s_h[w];
+        s_h[w] = 0;
+      }
+      if (c) atomicAdd(&g[i], c);
+    }
     __syncthreads();
+  };
+  for (uint32_t t = t0; t < t1; ++t) {
+    if (seg + 1 < p.nseg && t >= p.seg_tile_start[seg + 1]) {
+      flush(seg);
+      while (seg + 1 < p.nseg && t >= p.seg_tile_start[seg + 1]) ++seg;
+    }
+    const uint64_t b = p.seg_range[2 * seg] + uint64_t(t - p.seg_tile_start[seg]) * p.tile;
+    const uint64_t e = min(b + p.tile, p.seg_range[2 * seg + 1]);
+    // Keys before the first 16-byte boundary and after the last one one at a
+    // time; the rest as 16-byte vectors.
+    const uint64_t lead = (KPV - (b & (KPV - 1))) & (KPV - 1);
+    const uint64_t head = vec && lead < e - b ? lead : e - b;
+    const uint32_t nvec = uint32_t((e - b - head) / KPV);
+    const uint64_t tail = b + head + uint64_t(nvec) * KPV;
+    for (uint64_t i = b + tid; i < b + head; i += SEG_HIST_THREADS) count(kx.fwd(keys[i]));
+    for (uint64_t i = tail + tid; i < e; i += SEG_HIST_THREADS) count(kx.fwd(keys[i]));
+    const uint4* kv = reinterpret_cast<const uint4*>(keys + b + head);
+    for (uint32_t v0 = tid; v0 < nvec; v0 += SEG_HIST_THREADS * SEG_HIST_UNROLL) {
+      uint4 q[SEG_HIST_UNROLL];
+#pragma unroll
+      for (int u = 0; u < SEG_HIST_UNROLL; ++u) {
+        const uint32_t vi = v0 + u * SEG_HIST_THREADS;
+        q[u] = vi < nvec ? kv[vi] : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < SEG_HIST_UNROLL; ++u) {
+        if (v0 + u * SEG_HIST_THREADS < nvec) {
+          if constexpr (KPV == 4) {
+            count(kx.fwd(K(q[u].x)));
+            count(kx.fwd(K(q[u].y)));
+            count(kx.fwd(K(q[u].z)));
+            count(kx.fwd(K(q[u].w)));
+          } else {
+            count(kx.fwd(K(q[u].x) | (K(q[u].y) << 32)));
+            count(kx.fwd(K(q[u].z) | (K(q[u].w) << 32)));
+          }
+        }
+      }
+    }
   }
+  flush(seg);
 }
 
 // In place: histogram -> exclusive bin bases, one block per segment.
@@ -296,6 +366,7 @@ struct gs_seg_plan {
   gs::TinySeg* d_tiny = nullptr;
   uint32_t* d_starts_rel = nullptr;
   uint32_t* d_tile_start = nullptr;
+  gs::SegTile* d_tiles = nullptr;
   uint64_t* d_range = nullptr;
   uint32_t* d_hist = nullptr;
   gs::SortWork* d_work = nullptr;
@@ -318,6 +389,7 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
   std::vector<TinySeg> tiny;
   std::vector<uint32_t> rel;
   std::vector<uint32_t> tile_start;
+  std::vector<SegTile> tile_desc;
   std::vector<uint64_t> range;
   SegGroup cur{};
   uint32_t cur_max = 0;  // longest segment of the open group
@@ -348,8 +420,11 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
     if (len > GROUP_KEYS) {
       close();
       tile_start.push_back(uint32_t(tiles));
+      const uint32_t large_index = uint32_t(range.size() / 2);
       range.push_back(b);
       range.push_back(e);
+      for (uint64_t x = b; x < e; x += pl->tile)
+        tile_desc.push_back(SegTile{x, uint32_t(std::min<uint64_t>(pl->tile, e - x)), large_index});
       tiles += (len + pl->tile - 1) / pl->tile;
       continue;
     }
@@ -381,6 +456,7 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
             up(reinterpret_cast<void**>(&pl->d_tiny), tiny.data(), tiny.size() * sizeof(TinySeg)) &&
             up(reinterpret_cast<void**>(&pl->d_starts_rel), rel.data(), rel.size() * 4) &&
             up(reinterpret_cast<void**>(&pl->d_tile_start), tile_start.data(), tile_start.size() * 4) &&
+            up(reinterpret_cast<void**>(&pl->d_tiles), tile_desc.data(), tile_desc.size() * sizeof(SegTile)) &&
             up(reinterpret_cast<void**>(&pl->d_range), range.data(), range.size() * 8);
   if (ok && pl->nlarge) {
     ok = cudaMalloc(&pl->d_hist, size_t(pl->nlarge) * key_bytes * RADIX * 4) == cudaSuccess &&
@@ -394,8 +470,8 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
 }
 
 void seg_plan_free(gs_seg_plan* pl) {
-  void* ps[] = {pl->d_groups, pl->d_tiny, pl->d_starts_rel, pl->d_tile_start, pl->d_range,
-                pl->d_hist, pl->d_work};
+  void* ps[] = {pl->d_groups, pl->d_tiny, pl->d_starts_rel, pl->d_tile_start, pl->d_tiles,
+                pl->d_range, pl->d_hist, pl->d_work};
   for (void* p : ps)
     if (p) cudaFree(p);
   delete pl;
@@ -432,8 +508,11 @@ cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* al
   if (e != cudaSuccess) return e;
   SegHistParams hp{in, pl->d_tile_start, pl->d_range, pl->nlarge, pl->tile, pl->large_tiles,
                    pl->kind, pl->desc, pl->d_hist};
-  unsigned hb = std::min<unsigned>(pl->large_tiles, unsigned(props.num_sms) * 8);
-  seg_hist_kernel<K><<<hb, 256, 0, st>>>(hp);
+  // Six CTAs per SM (32 KB of counters each).
+  unsigned hb = std::min<unsigned>(pl->large_tiles, unsigned(props.num_sms) * 6);
+  e = allow_dynamic_smem(reinterpret_cast<const void*>(seg_hist_kernel<K>), seg_hist_smem<K>());
+  if (e != cudaSuccess) return e;
+  seg_hist_kernel<K><<<hb, SEG_HIST_THREADS, seg_hist_smem<K>(), st>>>(hp);
   seg_scan_kernel<<<pl->nlarge, 256, 0, st>>>(pl->d_hist, digits);
   seg_plan_kernel<<<1, 32, 0, st>>>(pl->d_work, digits, gen_counter);
   e = cudaGetLastError();
@@ -453,7 +532,8 @@ cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* al
   job.spin_limit = spin_limit;
   job.shape = pl->shape;
   job.gen_counter = gen_counter;
-  SegJob sj{pl->d_tile_start, pl->d_range, pl->d_hist, pl->nlarge, digits, pl->large_tiles};
+  SegJob sj{pl->d_tile_start, pl->d_range, pl->d_hist, pl->nlarge, digits, pl->large_tiles,
+            pl->d_tiles};
   uint32_t unused = 0;
   return launch_radix_passes(job, sj, props, &unused, st);
 }
