@@ -88,9 +88,24 @@ struct GroupSortParams {
 };
 
 // One CTA sorts one group in shared memory: LSD passes over the key's
-// digits (stable ranking with shared peer masks, as in the pass kernel;
-// the first pass may be unstable), then one pass over the local segment id
-// when the group holds several segments.
+// digits, then one pass over the local segment id when the group holds
+// several segments. The first key pass ranks unstably (a digit count per
+// key, then an atomic on the digit's running offset places it): equal
+// digits there are either equal keys of one segment, which cannot be told
+// apart, or are ordered by a later pass. The later passes rank stably with
+// per-warp peer masks, as the pass kernel's table ranking does.
+//
+// Shared memory: two buffer sets {keys, 8-bit segment ids} (the source and
+// the destination of a pass), then per-warp digit offsets. The ranking
+// table of a stable pass lives in the destination set, which the pass
+// writes only after the table's counts became offsets. 32-bit keys: 48 KB,
+// four CTAs per SM.
+template <typename K>
+__host__ __device__ constexpr size_t group_set_bytes() {
+  return (size_t(GROUP_KEYS) * (sizeof(K) + 1) + 15) & ~size_t(15);
+}
+constexpr size_t GROUP_OFF_BYTES = size_t(GROUP_THREADS / 32) * RADIX * sizeof(uint16_t);
+
 template <typename K>
 __global__ void __launch_bounds__(GROUP_THREADS)
 group_sort_kernel(GroupSortParams p) {
@@ -98,12 +113,14 @@ group_sort_kernel(GroupSortParams p) {
   constexpr int ITEMS = GROUP_ITEMS;
   constexpr int WARPS = THREADS / 32;
   constexpr int TILE = GROUP_KEYS;
-  // Dynamic: two key buffers, then two segment-id buffers.
+  constexpr size_t SET = group_set_bytes<K>();
+  static_assert(size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t) <= SET, "table fits a buffer set");
+  static_assert(GROUP_MAX_SEGS <= 256, "segment ids are one byte");
   extern __shared__ __align__(16) uint8_t s_dyn[];
-  K* s_key[2] = {reinterpret_cast<K*>(s_dyn), reinterpret_cast<K*>(s_dyn) + TILE};
-  uint16_t* s_sid[2] = {reinterpret_cast<uint16_t*>(s_dyn + 2 * TILE * sizeof(K)),
-                        reinterpret_cast<uint16_t*>(s_dyn + 2 * TILE * sizeof(K)) + TILE};
-  __shared__ __align__(16) uint64_t s_tab[WARPS][RADIX + 1];
+  auto set_keys = [&](int b) { return reinterpret_cast<K*>(s_dyn + b * SET); };
+  auto set_sid = [&](int b) { return s_dyn + b * SET + size_t(TILE) * sizeof(K); };
+  uint16_t (*const s_off)[RADIX] = reinterpret_cast<uint16_t (*)[RADIX]>(s_dyn + 2 * SET);
+  uint32_t* const s_cnt = reinterpret_cast<uint32_t*>(s_dyn + 2 * SET);  // unstable pass
   __shared__ uint32_t s_sstart[GROUP_MAX_SEGS + 1];
   __shared__ uint32_t s_tmp[8];
 
@@ -118,15 +135,19 @@ group_sort_kernel(GroupSortParams p) {
   for (uint32_t i = tid; i <= g.nsegs; i += THREADS)
     s_sstart[i] = p.groups ? p.seg_starts_rel[g.first_seg + i] : (i == 0 ? 0u : cnt);
   __syncthreads();
-  // Load (transformed) keys and local segment ids.
-  for (uint32_t i = tid; i < cnt; i += THREADS) {
-    s_key[0][i] = kx.fwd(in[i]);
-    uint32_t lo = 0, hi = g.nsegs;  // last s with s_sstart[s] <= i
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (s_sstart[mid] <= i) lo = mid; else hi = mid;
+  // Load (transformed) keys and local segment ids into set 0.
+  {
+    K* k0 = set_keys(0);
+    uint8_t* d0 = set_sid(0);
+    for (uint32_t i = tid; i < cnt; i += THREADS) {
+      k0[i] = kx.fwd(in[i]);
+      uint32_t lo = 0, hi = g.nsegs;  // last s with s_sstart[s] <= i
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_sstart[mid] <= i) lo = mid; else hi = mid;
+      }
+      d0[i] = uint8_t(lo);
     }
-    s_sid[0][i] = uint16_t(lo);
   }
   const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;
   const uint32_t lt = lanemask_lt();
@@ -135,72 +156,103 @@ group_sort_kernel(GroupSortParams p) {
   int cur = 0;
   for (int q = 0; q < passes; ++q) {
     const bool sid_pass = q == key_digits;
+    const bool unstable = q == 0;
     const uint32_t shift = RADIX_BITS * uint32_t(q);
-    for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&s_tab[0][0])[i] = 0ull;
+    const K* src_k = set_keys(cur);
+    const uint8_t* src_s = set_sid(cur);
+    K* dst_k = set_keys(cur ^ 1);
+    uint8_t* dst_s = set_sid(cur ^ 1);
+    uint64_t (*const tab)[RADIX + 1] = reinterpret_cast<uint64_t (*)[RADIX + 1]>(s_dyn + (cur ^ 1) * SET);
+    if (unstable) {
+      if (tid < RADIX) s_cnt[tid] = 0u;
+    } else {
+      for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&tab[0][0])[i] = 0ull;
+    }
     __syncthreads();
     K keys[ITEMS];
-    uint32_t rank2[ITEMS / 2];
-#pragma unroll
-    for (int i = 0; i < ITEMS / 2; ++i) rank2[i] = 0;
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
       const uint32_t l = wloc + 32 * i;
-      keys[i] = l < cnt ? s_key[cur][l] : K(0);
+      keys[i] = l < cnt ? src_k[l] : K(0);
     }
     auto digit_at = [&](int i) -> uint32_t {
-      return sid_pass ? uint32_t(s_sid[cur][wloc + 32 * i])
-                      : (uint32_t(keys[i] >> shift) & (RADIX - 1));
+      return sid_pass ? uint32_t(src_s[wloc + 32 * i]) : (uint32_t(keys[i] >> shift) & (RADIX - 1));
     };
-    uint64_t* tab = s_tab[warp];
+    if (unstable) {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+        if (wloc + 32 * i < cnt) atomicAdd(&s_cnt[digit_at(i)], 1u);
+      __syncthreads();
+      const uint32_t c = tid < RADIX ? s_cnt[tid] : 0u;
+      const uint32_t excl = block_excl_scan_256(c, s_tmp);
+      if (tid < RADIX) s_cnt[tid] = excl;  // the digit's running offset
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t l = wloc + 32 * i;
+        if (l < cnt) {
+          const uint32_t pos = atomicAdd(&s_cnt[digit_at(i)], 1u);
+          dst_k[pos] = keys[i];
+          dst_s[pos] = src_s[l];
+        }
+      }
+      __syncthreads();
+      cur ^= 1;
+      continue;
+    }
+    uint32_t rank2[ITEMS / 2];
+#pragma unroll
+    for (int i = 0; i < ITEMS / 2; ++i) rank2[i] = 0;
+    uint64_t* wt = tab[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
       const uint32_t d = (wloc + 32 * i < cnt) ? digit_at(i) : uint32_t(RADIX);
-      atomicOr(reinterpret_cast<uint32_t*>(&tab[d]), 1u << lane);
+      atomicOr(reinterpret_cast<uint32_t*>(&wt[d]), 1u << lane);
       __syncwarp();
-      const uint64_t e = tab[d];
+      const uint64_t e = wt[d];
       __syncwarp();
       const uint32_t peers = uint32_t(e), below = peers & lt, base = uint32_t(e >> 32);
       rank2[i >> 1] |= (base + __popc(below)) << (16 * (i & 1));
-      if (below == 0) tab[d] = uint64_t(base + __popc(peers)) << 32;
+      if (below == 0) wt[d] = uint64_t(base + __popc(peers)) << 32;
       __syncwarp();
     }
     __syncthreads();
     uint32_t count = 0;
     if (tid < RADIX) {
-      uint32_t run = 0;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) {
-        const uint32_t c = uint32_t(s_tab[w][tid] >> 32);
-        s_tab[w][tid] = run;
-        run += c;
-      }
-      count = run;
+      for (int w = 0; w < WARPS; ++w) count += uint32_t(tab[w][tid] >> 32);
     }
     const uint32_t excl = block_excl_scan_256(count, s_tmp);
     if (tid < RADIX) {
+      uint32_t run = excl;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) s_tab[w][tid] += excl;
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = uint32_t(tab[w][tid] >> 32);
+        s_off[w][tid] = uint16_t(run);
+        run += c;
+      }
     }
-    __syncthreads();
-    const uint32_t* off = reinterpret_cast<const uint32_t*>(&s_tab[warp][0]);
+    __syncthreads();  // the table's counts are read: the destination set is free
+    const uint16_t* off = s_off[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
       const uint32_t l = wloc + 32 * i;
       if (l < cnt) {
-        const uint32_t pos = off[2 * digit_at(i)] + ((rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu);
-        s_key[cur ^ 1][pos] = keys[i];
-        s_sid[cur ^ 1][pos] = s_sid[cur][l];
+        const uint32_t pos = off[digit_at(i)] + ((rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu);
+        dst_k[pos] = keys[i];
+        dst_s[pos] = src_s[l];
       }
     }
     __syncthreads();
     cur ^= 1;
   }
-  for (uint32_t i = tid; i < cnt; i += THREADS) out[i] = kx.inv(s_key[cur][i]);
+  const K* res = set_keys(cur);
+  for (uint32_t i = tid; i < cnt; i += THREADS) out[i] = kx.inv(res[i]);
 }
 
 template <typename K>
 constexpr size_t group_sort_dyn_smem() {
-  return 2 * size_t(GROUP_KEYS) * (sizeof(K) + sizeof(uint16_t));
+  return 2 * group_set_bytes<K>() + GROUP_OFF_BYTES;
 }
 
 // Histograms of every digit, per large segment.
