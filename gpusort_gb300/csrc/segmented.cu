@@ -268,16 +268,17 @@ struct SegHistParams {
   uint32_t* hist;       // [nseg][digits][RADIX]
 };
 
-// Each CTA takes a contiguous run of tiles, so consecutive tiles mostly
-// belong to one segment: the CTA counts into shared memory and adds its
-// counts to the segment's histogram only when the segment changes, and at
-// the end. Every bin has SEG_HIST_COLS columns, lane l counting into column
-// l mod SEG_HIST_COLS, so a warp's atomics to random bins spread over more
-// banks. (100,000 segments, ~2^30 u32 keys: one counter per bin, tiles
-// strided over the grid and a flush per tile took 2.3 ms.)
-constexpr int SEG_HIST_THREADS = 256;
-constexpr int SEG_HIST_UNROLL = 3;  // 16-byte vectors in flight per thread
-template <typename K> __host__ __device__ constexpr int seg_hist_cols() { return sizeof(K) == 4 ? 8 : 4; }
+// One 1024-thread CTA per SM takes a contiguous run of tiles and, for each
+// segment the run meets, counts that segment's keys in the run (16-byte
+// loads between the range's 16-byte boundaries) into shared memory, then
+// adds the counts to the segment's histogram. Every bin has one column per
+// lane for 32-bit keys (16 for 64-bit keys), as in the upsweep, so a
+// warp's atomics to random bins do not share banks. (100,000 segments,
+// ~2^30 u32 keys: 2.3 ms with one counter per bin, tiles strided over the
+// grid and a flush per tile; 1.76 ms with 8 columns in 256-thread CTAs.)
+constexpr int SEG_HIST_THREADS = 1024;
+constexpr int SEG_HIST_UNROLL = 4;  // 16-byte vectors in flight per thread
+template <typename K> __host__ __device__ constexpr int seg_hist_cols() { return sizeof(K) == 4 ? 32 : 16; }
 template <typename K> constexpr size_t seg_hist_smem() {
   return size_t(Bits<K>::DIGITS) * RADIX * seg_hist_cols<K>() * sizeof(uint32_t);
 }
@@ -287,12 +288,12 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) seg_hist_kernel(SegHistParam
   constexpr int KD = Bits<K>::DIGITS;
   constexpr uint32_t NC = seg_hist_cols<K>();
   constexpr uint32_t WORDS = KD * RADIX * NC;
+  constexpr uint32_t KPV = 16 / sizeof(K);  // keys per 16-byte vector
   extern __shared__ __align__(16) uint32_t s_h[];  // [digit][bin][column]
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const K* keys = static_cast<const K*>(p.keys);
   const uint32_t tid = threadIdx.x;
   uint32_t* const hk = s_h + (tid & (NC - 1));
-  constexpr uint32_t KPV = 16 / sizeof(K);  // keys per 16-byte vector
   const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
   auto count = [&](K v) {
 #pragma unroll
@@ -303,8 +304,7 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) seg_hist_kernel(SegHistParam
   const uint32_t t1 = min(t0 + per, p.total_tiles);
   if (t0 >= t1) return;
   for (uint32_t i = tid; i < WORDS; i += SEG_HIST_THREADS) s_h[i] = 0;
-  // The segment of tile t0: the last s with seg_tile_start[s] <= t0 (every
-  // thread finds the same one).
+  // The segment of tile t0: the last s with seg_tile_start[s] <= t0.
   uint32_t seg = 0;
   {
     uint32_t lo = 0, hi = p.nseg;
@@ -315,47 +315,30 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) seg_hist_kernel(SegHistParam
     seg = lo;
   }
   __syncthreads();
-  auto flush = [&](uint32_t s) {
-    __syncthreads();
-    uint32_t* g = p.hist + size_t(s) * KD * RADIX;
-    for (uint32_t i = tid; i < uint32_t(KD * RADIX); i += SEG_HIST_THREADS) {
-      uint32_t c = 0;
-#pragma unroll
-      for (uint32_t j = 0; j < NC; ++j) {
-        const uint32_t w = i * NC + ((j + i) & (NC - 1));
-        c += s_h[w];
-        s_h[w] = 0;
-      }
-      if (c) atomicAdd(&g[i], c);
-    }
-    __syncthreads();
-  };
-  for (uint32_t t = t0; t < t1; ++t) {
-    if (seg + 1 < p.nseg && t >= p.seg_tile_start[seg + 1]) {
-      flush(seg);
-      while (seg + 1 < p.nseg && t >= p.seg_tile_start[seg + 1]) ++seg;
-    }
-    const uint64_t b = p.seg_range[2 * seg] + uint64_t(t - p.seg_tile_start[seg]) * p.tile;
-    const uint64_t e = min(b + p.tile, p.seg_range[2 * seg + 1]);
-    // Keys before the first 16-byte boundary and after the last one one at a
-    // time; the rest as 16-byte vectors.
+  while (true) {
+    // This run's tiles of segment seg, and their elements [b, e).
+    const uint32_t f = p.seg_tile_start[seg];
+    const uint32_t ta = max(t0, f), tb = min(t1, p.seg_tile_start[seg + 1]);
+    const uint64_t s0 = p.seg_range[2 * seg], s1 = p.seg_range[2 * seg + 1];
+    const uint64_t b = s0 + uint64_t(ta - f) * p.tile;
+    const uint64_t e = min(s0 + uint64_t(tb - f) * p.tile, s1);
     const uint64_t lead = (KPV - (b & (KPV - 1))) & (KPV - 1);
     const uint64_t head = vec && lead < e - b ? lead : e - b;
-    const uint32_t nvec = uint32_t((e - b - head) / KPV);
-    const uint64_t tail = b + head + uint64_t(nvec) * KPV;
+    const uint64_t nvec = (e - b - head) / KPV;
+    const uint64_t tail = b + head + nvec * KPV;
     for (uint64_t i = b + tid; i < b + head; i += SEG_HIST_THREADS) count(kx.fwd(keys[i]));
     for (uint64_t i = tail + tid; i < e; i += SEG_HIST_THREADS) count(kx.fwd(keys[i]));
     const uint4* kv = reinterpret_cast<const uint4*>(keys + b + head);
-    for (uint32_t v0 = tid; v0 < nvec; v0 += SEG_HIST_THREADS * SEG_HIST_UNROLL) {
+    for (uint64_t v0 = tid; v0 < nvec; v0 += uint64_t(SEG_HIST_THREADS) * SEG_HIST_UNROLL) {
       uint4 q[SEG_HIST_UNROLL];
 #pragma unroll
       for (int u = 0; u < SEG_HIST_UNROLL; ++u) {
-        const uint32_t vi = v0 + u * SEG_HIST_THREADS;
+        const uint64_t vi = v0 + uint64_t(u) * SEG_HIST_THREADS;
         q[u] = vi < nvec ? kv[vi] : make_uint4(0, 0, 0, 0);
       }
 #pragma unroll
       for (int u = 0; u < SEG_HIST_UNROLL; ++u) {
-        if (v0 + u * SEG_HIST_THREADS < nvec) {
+        if (v0 + uint64_t(u) * SEG_HIST_THREADS < nvec) {
           if constexpr (KPV == 4) {
             count(kx.fwd(K(q[u].x)));
             count(kx.fwd(K(q[u].y)));
@@ -368,8 +351,23 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) seg_hist_kernel(SegHistParam
         }
       }
     }
+    // Add the counts to the segment's histogram and clear them.
+    __syncthreads();
+    uint32_t* g = p.hist + size_t(seg) * KD * RADIX;
+    for (uint32_t i = tid; i < uint32_t(KD * RADIX); i += SEG_HIST_THREADS) {
+      uint32_t c = 0;
+#pragma unroll
+      for (uint32_t j = 0; j < NC; ++j) {
+        const uint32_t w = i * NC + ((j + i) & (NC - 1));
+        c += s_h[w];
+        s_h[w] = 0;
+      }
+      if (c) atomicAdd(&g[i], c);
+    }
+    __syncthreads();
+    if (tb >= t1 || seg + 1 >= p.nseg) break;
+    ++seg;
   }
-  flush(seg);
 }
 
 // In place: histogram -> exclusive bin bases, one block per segment.
@@ -560,8 +558,8 @@ cudaError_t seg_run_t(const gs_seg_plan* pl, const void* in, void* out, void* al
   if (e != cudaSuccess) return e;
   SegHistParams hp{in, pl->d_tile_start, pl->d_range, pl->nlarge, pl->tile, pl->large_tiles,
                    pl->kind, pl->desc, pl->d_hist};
-  // Six CTAs per SM (32 KB of counters each).
-  unsigned hb = std::min<unsigned>(pl->large_tiles, unsigned(props.num_sms) * 6);
+  // One CTA per SM (128 KB of counters).
+  unsigned hb = std::min<unsigned>(pl->large_tiles, unsigned(props.num_sms));
   e = allow_dynamic_smem(reinterpret_cast<const void*>(seg_hist_kernel<K>), seg_hist_smem<K>());
   if (e != cudaSuccess) return e;
   seg_hist_kernel<K><<<hb, SEG_HIST_THREADS, seg_hist_smem<K>(), st>>>(hp);
