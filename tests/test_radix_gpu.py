@@ -55,6 +55,24 @@ def test_keys_large_adversarial(ctx, dtype, dist):
         assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc)), (dtype, dist, desc)
 
 
+@pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.uint64])
+@pytest.mark.parametrize("mask_kind", ["low8", "low16", "mid8", "low24"])
+def test_keys_constant_digits(ctx, dtype, mask_kind):
+    """Digits shared by every key are skipped, so the first pass that runs is
+    a higher digit's (the lowest digit's own kernel does not run) or a
+    later pass follows a skipped one: keys with the low byte(s) or a middle
+    byte cleared, over several tiles, both orders."""
+    bits = np.dtype(dtype).itemsize * 8
+    u = np.dtype(f"u{bits // 8}")
+    keep = {"low8": ~np.uint64(0xFF), "low16": ~np.uint64(0xFFFF), "mid8": ~np.uint64(0xFF00),
+            "low24": ~np.uint64(0xFFFFFF)}[mask_kind]
+    for i, n in enumerate([4097, (1 << 21) + 333]):
+        r = datagen.host("uniform", n, u, seed=60 + i).astype(np.uint64)
+        a = (r & keep).astype(u).view(dtype)
+        for desc in (False, True):
+            assert same_bits(_sort(ctx, a, desc), oracle.sort_keys(a, desc)), (dtype, mask_kind, n, desc)
+
+
 @pytest.mark.parametrize("dtype", [np.uint32, np.float64, np.int32])
 @pytest.mark.parametrize("dist", ["uniform", "equal", "distinct8"])
 def test_keys_in_place(ctx, dtype, dist):
@@ -117,6 +135,22 @@ def test_pairs(ctx, kt, vt, stable):
                 gk, gv = _pairs(ctx, k, v, desc, stable, in_place=(i == 3))
                 wk, wv = oracle.sort_pairs(k, v, desc, stable)
                 assert same_bits(gk, wk) and same_bits(gv, wv), (kt, vt, n, dist, desc, stable)
+
+
+@pytest.mark.parametrize("kt,vt", [(np.uint32, np.uint32), (np.uint64, np.uint32)])
+@pytest.mark.parametrize("stable", [False, True])
+def test_pairs_constant_low_key_digit(ctx, kt, vt, stable):
+    """Keys with the low byte cleared: the key's lowest digit is skipped,
+    after the value digits (ties by value) or first (index payload)."""
+    n = (1 << 20) + 4097
+    u = np.dtype(f"u{np.dtype(kt).itemsize}")
+    k = (datagen.host("uniform", n, u, seed=71).astype(np.uint64) & ~np.uint64(0xFF)).astype(u).view(kt)
+    v = (np.arange(n, dtype=np.uint64).astype(vt) if stable
+         else datagen.host("distinct8", n, vt, seed=72))
+    for desc in (False, True):
+        gk, gv = _pairs(ctx, k, v, desc, stable)
+        wk, wv = oracle.sort_pairs(k, v, desc, stable)
+        assert same_bits(gk, wk) and same_bits(gv, wv), (kt, vt, desc, stable)
 
 
 @pytest.mark.parametrize("kt,vt", [(np.uint32, np.uint32), (np.int64, np.uint32),
