@@ -112,7 +112,11 @@ gs_status check_err_word(gs_ctx* ctx) {
   if (h) {
     cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream);
     cudaStreamSynchronize(ctx->stream);
-    std::string m = "device wait ran out or scatter out of range (code " + std::to_string(h) + ")";
+    std::string m = "device error (code " + std::to_string(h) + "):";
+    if (h & gs::ERR_LOOKBACK_TIMEOUT) m += " look-back wait ran out;";
+    if (h & gs::ERR_SCATTER_RANGE) m += " scatter range left the output;";
+    if (h & gs::ERR_PASS_KIND) m += " unstable-only pass kernel launched for a stable pass;";
+    if (h & gs::ERR_SMEM_ALIGN) m += " shared memory misaligned;";
     return fail(ctx, GS_ERR_TIMEOUT, m);
   }
   if (ctx->timing && ctx->n_phases > 0) {
