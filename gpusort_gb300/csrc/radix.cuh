@@ -406,8 +406,6 @@ pass_kernel(PassParams p) {
   const OrderXform<K> kx(p.key_kind, p.desc != 0);
   const OrderXform<VS> vx(p.val_kind, p.desc != 0);
 
-  // Tiles are claimed in launch order, so a tile only ever waits on tiles
-  // held by CTAs that are already running.
   // L2 prefetch of the elements prefetch_tiles tiles further on, which a
   // CTA claims about when this one finishes (segmented sorts: the same
   // distance in elements, a hint that may cross into later segments).
@@ -422,6 +420,8 @@ pass_kernel(PassParams p) {
       if constexpr (HAS_V) pf(src_v + b, c * sizeof(VS));
     }
   };
+  // Tiles are claimed in launch order, so a tile only ever waits on tiles
+  // held by CTAs that are already running.
   if (tid == 0) {
     const uint32_t t = atomicAdd(&plan.tile_counter[p.pass], 1u);
     s_tile = t;
@@ -431,9 +431,10 @@ pass_kernel(PassParams p) {
   }
   if ((smem_addr(s_dyn) & 15u) == 0) {
     uint4* z = reinterpret_cast<uint4*>(s_dyn);
-    // The unstable ranking uses only the first RADIX words. (Only the
-    // keys-only table kernels, which run the lowest digit's unstable pass,
-    // skip the rest: the same branch costs the other kernels registers.)
+    // The unstable ranking uses only the first RADIX words: the
+    // RANK_UNSTABLE kernel clears only those, and so do the keys-only table
+    // kernels when they rank a sort's first pass unstably (the same branch
+    // costs the other kernels registers).
     if (RANK == RANK_UNSTABLE || (!HAS_V && RANK == RANK_TABLE && unstable)) {
       if (tid < RADIX / 4) z[tid] = make_uint4(0, 0, 0, 0);
     } else {
