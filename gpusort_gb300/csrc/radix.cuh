@@ -90,7 +90,8 @@ upsweep_kernel(UpsweepParams p) {
   const uint64_t chunk = uint64_t(THREADS) * UNROLL;
   K* const copy_k = static_cast<K*>(p.copy_keys);
   // Keys only: interior chunks are read as 16-byte vectors when the
-  // buffers are 16-byte aligned (2^30 u32 keys: 1.00 -> 0.82 ms).
+  // buffers are 16-byte aligned (2^30 u32 keys: 1.00 -> 0.86 ms), the next
+  // chunk's loads in flight while this one is counted (0.86 -> 0.82 ms).
   constexpr int KPV = int(16 / sizeof(K));  // keys per vector
   constexpr bool VEC = !HAS_V && UNROLL % KPV == 0;
   const bool vec = VEC && (reinterpret_cast<uintptr_t>(keys) & 15u) == 0 &&
@@ -152,26 +153,37 @@ upsweep_kernel(UpsweepParams p) {
       }
     }
   };
-  for (uint64_t base = uint64_t(blockIdx.x) * chunk; base < n;
-       base += uint64_t(gridDim.x) * chunk) {
-    K k[UNROLL];
-    bool valid[UNROLL];
-    if (VEC && vec && base + chunk <= n) {
-      // Interior chunk, keys only: thread t's items are the keys of 16-byte
-      // vectors t, t + THREADS, ... (the order of a histogram's counts does
-      // not matter).
-      const uint32_t* kb = reinterpret_cast<const uint32_t*>(keys + base);
+  uint64_t base = uint64_t(blockIdx.x) * chunk;
+  const uint64_t stride = uint64_t(gridDim.x) * chunk;
+  if (VEC && vec) {
+    // Interior chunks, keys only, software-pipelined: the next chunk's
+    // vectors load while this one's keys are counted. Thread t's items are
+    // the keys of 16-byte vectors t, t + THREADS, ... (the order of a
+    // histogram's counts does not matter).
+    constexpr int NV = UNROLL / KPV;
+    uint4 q[NV], qn[NV];
+    auto load = [&](uint64_t b, uint4 (&dst)[NV]) {
+      const uint32_t* kb = reinterpret_cast<const uint32_t*>(keys + b);
 #pragma unroll
-      for (int u = 0; u < UNROLL / KPV; ++u) {
-        const uint4 q = ld_stream_v4(kb + 4 * (u * THREADS + threadIdx.x));
+      for (int u = 0; u < NV; ++u) dst[u] = ld_stream_v4(kb + 4 * (u * THREADS + threadIdx.x));
+    };
+    if (base + chunk <= n) load(base, q);
+    while (base + chunk <= n) {
+      const uint64_t nb = base + stride;
+      const bool more = nb + chunk <= n;
+      if (more) load(nb, qn);
+      K k[UNROLL];
+      bool valid[UNROLL];
+#pragma unroll
+      for (int u = 0; u < NV; ++u) {
         if constexpr (KPV == 4) {
-          k[4 * u] = K(q.x);
-          k[4 * u + 1] = K(q.y);
-          k[4 * u + 2] = K(q.z);
-          k[4 * u + 3] = K(q.w);
+          k[4 * u] = K(q[u].x);
+          k[4 * u + 1] = K(q[u].y);
+          k[4 * u + 2] = K(q[u].z);
+          k[4 * u + 3] = K(q[u].w);
         } else {
-          k[2 * u] = K(q.x) | (K(q.y) << 32);
-          k[2 * u + 1] = K(q.z) | (K(q.w) << 32);
+          k[2 * u] = K(q[u].x) | (K(q[u].y) << 32);
+          k[2 * u + 1] = K(q[u].z) | (K(q[u].w) << 32);
         }
       }
 #pragma unroll
@@ -179,21 +191,19 @@ upsweep_kernel(UpsweepParams p) {
       if (copy_k) {
         uint32_t* cb = reinterpret_cast<uint32_t*>(copy_k + base);
 #pragma unroll
-        for (int u = 0; u < UNROLL / KPV; ++u) {
-          uint4 q;
-          if constexpr (KPV == 4) {
-            q = make_uint4(uint32_t(k[4 * u]), uint32_t(k[4 * u + 1]), uint32_t(k[4 * u + 2]),
-                           uint32_t(k[4 * u + 3]));
-          } else {
-            q = make_uint4(uint32_t(k[2 * u]), uint32_t(k[2 * u] >> 32), uint32_t(k[2 * u + 1]),
-                           uint32_t(k[2 * u + 1] >> 32));
-          }
-          *reinterpret_cast<uint4*>(cb + 4 * (u * THREADS + threadIdx.x)) = q;
-        }
+        for (int u = 0; u < NV; ++u)
+          *reinterpret_cast<uint4*>(cb + 4 * (u * THREADS + threadIdx.x)) = q[u];
       }
       count(k, valid);
-      continue;
+#pragma unroll
+      for (int u = 0; u < NV; ++u) q[u] = qn[u];
+      base = nb;
+      if (!more) break;
     }
+  }
+  for (; base < n; base += stride) {
+    K k[UNROLL];
+    bool valid[UNROLL];
     if (base + chunk <= n) {  // interior chunk: no bounds checks
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
