@@ -173,7 +173,6 @@ gs_status device_sort(gs_ctx* ctx, int kb, uint32_t kkind, int vb, uint32_t vkin
                       const void* kin, const void* vin, void* kout, void* vout,
                       uint64_t n, uint32_t flags, const HostFuse* fuse = nullptr) {
   const bool desc = flags & GS_FLAG_DESCENDING;
-  const bool stable = flags & GS_FLAG_PAIRS_STABLE;
   // Few keys and no payload: one CTA sorts them in shared memory (one launch
   // instead of the radix pipeline's five). An explicit pass shape, timing
   // marks or an injected stall ask for the radix pipeline itself.

@@ -360,9 +360,9 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
                           const DeviceProps& props, cudaStream_t st) {
   // 16 (32-bit keys) or 12 (64-bit keys) items per thread leave registers
   // for the packed bucket ids.
-  using Sh = Shape<512, sizeof(K) == 4 ? 16 : 12, 2>;
   // The bucket scatter ranks unstably: the unstable-only kernel.
-  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS, RANK_UNSTABLE>;
+  using Sh = Shape<512, sizeof(K) == 4 ? 16 : 12, 2, RANK_UNSTABLE>;
+  using Cfg = PassConfig<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::RANK>;
   PlanParams pp{};
   pp.work = job.work;
   pp.gen_counter = job.gen_counter ? job.gen_counter : &job.work->gen_counter;
@@ -372,7 +372,7 @@ cudaError_t bucket_pass_t(const RadixJob& job, const void* splitters, uint32_t n
   pp.digit_lo = 0;
   pp.digit_hi = 1;
   plan_kernel<<<1, 256, 0, st>>>(pp);
-  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, RANK_UNSTABLE, true>;
+  auto kern = pass_kernel<K, NoValue, Sh::THREADS, Sh::ITEMS, Sh::MINB, Sh::RANK, true>;
   cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::DYN_SMEM_BUCKET);
   if (e != cudaSuccess) return e;
   PassParams pa{};
