@@ -94,6 +94,8 @@ constexpr int UPSWEEP_PER_SM = 3;
 // 4.30 ms with the 64-bit table; 2^29 pairs (same 384-thread tile, table vs
 // half-warp): u64 Zipf(1.1) + u32 index, stable, 33.6 -> 30.9 ms (skewed
 // digits), u64 + u32 uniform 50.0 -> 49.8 ms, u32 + u32 24.7 -> 24.3 ms.
+// u64 + u64 pairs keep the table in their 512-thread tile (2^28 pairs:
+// 38.7 ms vs 38.9 ms by half-warps).
 template <int T, int I, int B, int R = RANK_TABLE> struct Shape {
   static constexpr int THREADS = T, ITEMS = I, MINB = B, RANK = R;
 };
