@@ -93,18 +93,20 @@ struct GroupSortParams {
 // key, then an atomic on the digit's running offset places it): equal
 // digits there are either equal keys of one segment, which cannot be told
 // apart, or are ordered by a later pass. The later passes rank stably with
-// per-warp peer masks, as the pass kernel's table ranking does.
+// per-half-warp peer masks (16-bit mask and 16-bit count in one word), as
+// the pass kernel's half-warp ranking does; a half-warp's items are a
+// contiguous run of the group.
 //
 // Shared memory: two buffer sets {keys, 8-bit segment ids} (the source and
-// the destination of a pass), then per-warp digit offsets. The ranking
-// table of a stable pass lives in the destination set, which the pass
-// writes only after the table's counts became offsets. 32-bit keys: 48 KB,
-// four CTAs per SM.
+// the destination of a pass), then per-warp digit offsets (both halves'
+// in one word). The ranking table of a stable pass lives in the
+// destination set, which the pass writes only after the table's counts
+// became offsets. 32-bit keys: 48 KB, four CTAs per SM.
 template <typename K>
 __host__ __device__ constexpr size_t group_set_bytes() {
   return (size_t(GROUP_KEYS) * (sizeof(K) + 1) + 15) & ~size_t(15);
 }
-constexpr size_t GROUP_OFF_BYTES = size_t(GROUP_THREADS / 32) * RADIX * sizeof(uint16_t);
+constexpr size_t GROUP_OFF_BYTES = size_t(GROUP_THREADS / 32) * RADIX * sizeof(uint32_t);
 
 template <typename K>
 __global__ void __launch_bounds__(GROUP_THREADS)
@@ -114,12 +116,13 @@ group_sort_kernel(GroupSortParams p) {
   constexpr int WARPS = THREADS / 32;
   constexpr int TILE = GROUP_KEYS;
   constexpr size_t SET = group_set_bytes<K>();
-  static_assert(size_t(WARPS) * (RADIX + 1) * sizeof(uint64_t) <= SET, "table fits a buffer set");
+  static_assert(size_t(WARPS) * (RADIX + 1) * 2 * sizeof(uint32_t) <= SET, "table fits a buffer set");
+  static_assert(16 * ITEMS < 65536, "half-warp counts are 16-bit");
   static_assert(GROUP_MAX_SEGS <= 256, "segment ids are one byte");
   extern __shared__ __align__(16) uint8_t s_dyn[];
   auto set_keys = [&](int b) { return reinterpret_cast<K*>(s_dyn + b * SET); };
   auto set_sid = [&](int b) { return s_dyn + b * SET + size_t(TILE) * sizeof(K); };
-  uint16_t (*const s_off)[RADIX] = reinterpret_cast<uint16_t (*)[RADIX]>(s_dyn + 2 * SET);
+  uint32_t (*const s_off)[RADIX] = reinterpret_cast<uint32_t (*)[RADIX]>(s_dyn + 2 * SET);
   uint32_t* const s_cnt = reinterpret_cast<uint32_t*>(s_dyn + 2 * SET);  // unstable pass
   __shared__ uint32_t s_sstart[GROUP_MAX_SEGS + 1];
   __shared__ uint32_t s_tmp[8];
@@ -149,8 +152,12 @@ group_sort_kernel(GroupSortParams p) {
       d0[i] = uint8_t(lo);
     }
   }
-  const uint32_t wloc = uint32_t(warp) * 32 * ITEMS + lane;
-  const uint32_t lt = lanemask_lt();
+  // Item i of lane l is element wloc + 16 i: lanes 0-15 and 16-31 of a
+  // warp hold two consecutive runs of 16 * ITEMS elements.
+  const uint32_t h = uint32_t(lane) >> 4;
+  const uint32_t wloc = (2 * uint32_t(warp) + h) * 16 * ITEMS + (uint32_t(lane) & 15u);
+  const uint32_t lt = (1u << (uint32_t(lane) & 15u)) - 1u;
+  const uint32_t bit = 1u << (uint32_t(lane) & 15u);
   const int key_digits = int(sizeof(K));
   const int passes = key_digits + (g.nsegs > 1 ? 1 : 0);
   int cur = 0;
@@ -162,26 +169,27 @@ group_sort_kernel(GroupSortParams p) {
     const uint8_t* src_s = set_sid(cur);
     K* dst_k = set_keys(cur ^ 1);
     uint8_t* dst_s = set_sid(cur ^ 1);
-    uint64_t (*const tab)[RADIX + 1] = reinterpret_cast<uint64_t (*)[RADIX + 1]>(s_dyn + (cur ^ 1) * SET);
+    uint32_t (*const tab)[RADIX + 1][2] = reinterpret_cast<uint32_t (*)[RADIX + 1][2]>(s_dyn + (cur ^ 1) * SET);
     if (unstable) {
       if (tid < RADIX) s_cnt[tid] = 0u;
     } else {
-      for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) (&tab[0][0])[i] = 0ull;
+      uint64_t* z = reinterpret_cast<uint64_t*>(&tab[0][0][0]);
+      for (int i = tid; i < WARPS * (RADIX + 1); i += THREADS) z[i] = 0ull;
     }
     __syncthreads();
     K keys[ITEMS];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-      const uint32_t l = wloc + 32 * i;
+      const uint32_t l = wloc + 16 * i;
       keys[i] = l < cnt ? src_k[l] : K(0);
     }
     auto digit_at = [&](int i) -> uint32_t {
-      return sid_pass ? uint32_t(src_s[wloc + 32 * i]) : (uint32_t(keys[i] >> shift) & (RADIX - 1));
+      return sid_pass ? uint32_t(src_s[wloc + 16 * i]) : (uint32_t(keys[i] >> shift) & (RADIX - 1));
     };
     if (unstable) {
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i)
-        if (wloc + 32 * i < cnt) atomicAdd(&s_cnt[digit_at(i)], 1u);
+        if (wloc + 16 * i < cnt) atomicAdd(&s_cnt[digit_at(i)], 1u);
       __syncthreads();
       const uint32_t c = tid < RADIX ? s_cnt[tid] : 0u;
       const uint32_t excl = block_excl_scan_256(c, s_tmp);
@@ -189,7 +197,7 @@ group_sort_kernel(GroupSortParams p) {
       __syncthreads();
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t l = wloc + 32 * i;
+        const uint32_t l = wloc + 16 * i;
         if (l < cnt) {
           const uint32_t pos = atomicAdd(&s_cnt[digit_at(i)], 1u);
           dst_k[pos] = keys[i];
@@ -203,42 +211,47 @@ group_sort_kernel(GroupSortParams p) {
     uint32_t rank2[ITEMS / 2];
 #pragma unroll
     for (int i = 0; i < ITEMS / 2; ++i) rank2[i] = 0;
-    uint64_t* wt = tab[warp];
+    uint32_t (*const wt)[2] = tab[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-      const uint32_t d = (wloc + 32 * i < cnt) ? digit_at(i) : uint32_t(RADIX);
-      atomicOr(reinterpret_cast<uint32_t*>(&wt[d]), 1u << lane);
+      const uint32_t d = (wloc + 16 * i < cnt) ? digit_at(i) : uint32_t(RADIX);
+      uint32_t* e = &wt[d][h];
+      atomicOr(e, bit);
       __syncwarp();
-      const uint64_t e = wt[d];
+      const uint32_t w = *e;
       __syncwarp();
-      const uint32_t peers = uint32_t(e), below = peers & lt, base = uint32_t(e >> 32);
+      const uint32_t peers = w & 0xFFFFu, below = peers & lt, base = w >> 16;
       rank2[i >> 1] |= (base + __popc(below)) << (16 * (i & 1));
-      if (below == 0) wt[d] = uint64_t(base + __popc(peers)) << 32;
+      if (below == 0) *e = (base + __popc(peers)) << 16;
       __syncwarp();
     }
     __syncthreads();
     uint32_t count = 0;
     if (tid < RADIX) {
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) count += uint32_t(tab[w][tid] >> 32);
+      for (int w = 0; w < WARPS; ++w) {
+        const uint2 c = *reinterpret_cast<const uint2*>(&tab[w][tid][0]);
+        count += (c.x >> 16) + (c.y >> 16);
+      }
     }
     const uint32_t excl = block_excl_scan_256(count, s_tmp);
     if (tid < RADIX) {
       uint32_t run = excl;
 #pragma unroll
       for (int w = 0; w < WARPS; ++w) {
-        const uint32_t c = uint32_t(tab[w][tid] >> 32);
-        s_off[w][tid] = uint16_t(run);
-        run += c;
+        const uint2 c = *reinterpret_cast<const uint2*>(&tab[w][tid][0]);
+        const uint32_t c0 = c.x >> 16, c1 = c.y >> 16;
+        s_off[w][tid] = run | ((run + c0) << 16);
+        run += c0 + c1;
       }
     }
     __syncthreads();  // the table's counts are read: the destination set is free
-    const uint16_t* off = s_off[warp];
+    const uint32_t* off = s_off[warp];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-      const uint32_t l = wloc + 32 * i;
+      const uint32_t l = wloc + 16 * i;
       if (l < cnt) {
-        const uint32_t pos = off[digit_at(i)] + ((rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu);
+        const uint32_t pos = ((off[digit_at(i)] >> (16 * h)) & 0xFFFFu) + ((rank2[i >> 1] >> (16 * (i & 1))) & 0xFFFFu);
         dst_k[pos] = keys[i];
         dst_s[pos] = src_s[l];
       }
