@@ -53,6 +53,7 @@ EXPORTED = [
     "gs_segmented_sort_keys", "gs_gather", "gs_phase_times",
     "gs_ctx_set_timing", "gs_kernel_times", "gs_debug_set", "gs_sort_keys_noalloc",
     "gs_segmented_plan_create", "gs_segmented_plan_run", "gs_segmented_plan_destroy",
+    "gs_segmented_layout",
     "gs_server_create", "gs_server_destroy", "gs_server_submit", "gs_server_poll",
     "gs_server_cancel", "gs_server_get_stats",
     "gs_pass_shape_count", "gs_pass_shape_info", "gs_ctx_set_tuning", "gs_tuning_parse",
@@ -148,6 +149,8 @@ def load() -> C.CDLL:
         L.gs_segmented_plan_run.restype = i32
         L.gs_segmented_plan_destroy.argtypes = [vp]
         L.gs_segmented_plan_destroy.restype = None
+        L.gs_segmented_layout.argtypes = [i32, u64, vp, u32, vp, C.POINTER(u64)]
+        L.gs_segmented_layout.restype = i32
         L.gs_sort_keys_noalloc.argtypes = [i32, vp, vp, u64, u32, vp]
         L.gs_sort_keys_noalloc.restype = i32
         L.gs_pass_shape_count.restype = i32
@@ -212,6 +215,26 @@ def pass_shapes(key_bytes: int, val_bytes: int) -> list[tuple[int, int]]:
             raise GsError(GS_ERR_INVALID, "pass shape")
         out.append((t.value, it.value))
     return out
+
+
+SEG_EMPTY, SEG_WARP, SEG_GROUP, SEG_PASSES = 0, 1, 2, 3  # gs_seg_kind
+
+
+def segmented_layout(dtype, n: int, offsets) -> tuple[np.ndarray, dict]:
+    """gs_segmented_layout: the gs_seg_kind of each segment and the counts of
+    groups, warp-sorted segments, pass-sorted segments and pass tiles
+    (host only; no device needed)."""
+    L = load()
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    nseg = off.size - 1
+    kinds = np.zeros(max(1, nseg), dtype=np.uint8)
+    counts = (C.c_uint64 * 4)()
+    st = L.gs_segmented_layout(dtype_code(dtype), int(n), off.ctypes.data, nseg,
+                               kinds.ctypes.data, counts)
+    if st != GS_OK:
+        raise GsError(st, L.gs_last_global_error().decode())
+    keys = ("groups", "warp_segments", "pass_segments", "tiles")
+    return kinds[:nseg], {k: int(counts[i]) for i, k in enumerate(keys)}
 
 
 def tuning_parse(text: str) -> list[dict] | None:

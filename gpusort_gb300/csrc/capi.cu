@@ -695,6 +695,20 @@ gs_status gs_segmented_plan_create(gs_ctx* ctx, gs_dtype dtype, uint64_t n,
   return GS_OK;
 }
 
+gs_status gs_segmented_layout(gs_dtype dtype, uint64_t n, const uint64_t* host_offsets,
+                              uint32_t nseg, uint8_t* kinds, uint64_t counts[4]) {
+  int kb = 0;
+  uint32_t kk = 0;
+  if (!dtype_info(dtype, &kb, &kk)) return fail(nullptr, GS_ERR_BAD_DTYPE, "unknown key dtype");
+  if (n > MAX_N) return fail(nullptr, GS_ERR_TOO_LARGE, "n exceeds 2^32-1 elements");
+  if (!host_offsets || !counts) return fail(nullptr, GS_ERR_INVALID, "null argument");
+  const int shape = gs::radix_segmented_shape(kb, n, nseg);
+  const std::string err =
+      gs::seg_layout_summary(host_offsets, nseg, n, gs::radix_shape_tile(kb, 0, shape), kinds, counts);
+  if (!err.empty()) return fail(nullptr, GS_ERR_INVALID, err);
+  return GS_OK;
+}
+
 gs_status gs_segmented_plan_run(gs_ctx* ctx, const gs_seg_plan* plan, const void* in, void* out) {
   if (!ctx || !plan) return fail(ctx, GS_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lock(ctx->mu);

@@ -116,6 +116,10 @@ cudaError_t launch_radix_passes(const RadixJob& job, const SegJob& sj, const Dev
 struct gs_seg_plan;
 struct gs_ctx;
 namespace gs {
+// Host only: gs_segmented_layout's per-segment kinds and counts for pass
+// tiles of `tile` elements.
+std::string seg_layout_summary(const uint64_t* off, uint32_t nseg, uint64_t n, uint32_t tile,
+                               uint8_t* kinds, uint64_t counts[4]);
 std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, uint64_t n,
                            int key_bytes, uint32_t kind, bool desc, int shape);
 void seg_plan_free(gs_seg_plan* pl);

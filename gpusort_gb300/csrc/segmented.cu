@@ -437,6 +437,101 @@ struct gs_seg_plan {
 
 namespace gs {
 
+// How a segmented sort treats each segment (host only): small segments
+// packed in order into groups of consecutive segments (at most GROUP_KEYS
+// keys and GROUP_MAX_SEGS segments; a group made only of segments of at
+// most TINY_KEYS keys becomes one warp network per segment), and the large
+// segments cut into pass tiles of `tile` elements.
+struct SegLayout {
+  std::vector<SegGroup> groups;
+  std::vector<TinySeg> tiny;
+  std::vector<uint32_t> rel;         // per group: segment starts relative to the group
+  std::vector<uint32_t> tile_start;  // per large segment: first tile, then the tile count
+  std::vector<SegTile> tile_desc;    // per tile
+  std::vector<uint64_t> range;       // per large segment: [begin, end)
+  uint64_t tiles = 0;
+};
+
+// kinds (optional, nseg entries): the gs_seg_kind of each segment.
+std::string seg_layout(const uint64_t* off, uint32_t nseg, uint64_t n, uint32_t tile,
+                       SegLayout& L, uint8_t* kinds) {
+  if (off[0] != 0 || off[nseg] != n) return "offsets must start at 0 and end at n";
+  SegGroup cur{};
+  uint32_t cur_max = 0;    // longest segment of the open group
+  uint32_t cur_first = 0;  // index of the open group's first segment
+  bool open = false;
+  auto close = [&](uint32_t s_end) {  // s_end: the segment after the group's last
+    const bool is_tiny = open && cur.count > 0 && cur_max <= TINY_KEYS;
+    if (is_tiny) {
+      // Only tiny segments: one warp each instead of a group sort.
+      L.rel.push_back(cur.count);
+      for (uint32_t i = 0; i < cur.nsegs; ++i) {
+        const uint32_t a = L.rel[cur.first_seg + i], z = L.rel[cur.first_seg + i + 1];
+        L.tiny.push_back(TinySeg{cur.start + a, z - a, 0});
+      }
+      L.rel.resize(cur.first_seg);
+    } else if (open && cur.count > 0) {
+      L.rel.push_back(cur.count);  // end of the last segment
+      L.groups.push_back(cur);
+    } else if (open) {
+      L.rel.resize(cur.first_seg);  // empty group: drop its starts
+    }
+    if (kinds && open) {
+      for (uint32_t t = cur_first; t < s_end; ++t)
+        if (off[t + 1] > off[t]) kinds[t] = is_tiny ? GS_SEG_WARP : GS_SEG_GROUP;
+    }
+    open = false;
+  };
+  for (uint32_t s = 0; s < nseg; ++s) {
+    const uint64_t b = off[s], e = off[s + 1];
+    if (e < b) return "offsets must be non-decreasing";
+    const uint64_t len = e - b;
+    if (kinds) kinds[s] = GS_SEG_EMPTY;
+    if (len == 0) continue;  // nothing to move
+    if (len > GROUP_KEYS) {
+      close(s);
+      L.tile_start.push_back(uint32_t(L.tiles));
+      const uint32_t large_index = uint32_t(L.range.size() / 2);
+      L.range.push_back(b);
+      L.range.push_back(e);
+      for (uint64_t x = b; x < e; x += tile)
+        L.tile_desc.push_back(SegTile{x, uint32_t(std::min<uint64_t>(tile, e - x)), large_index});
+      L.tiles += (len + tile - 1) / tile;
+      if (kinds) kinds[s] = GS_SEG_PASSES;
+      continue;
+    }
+    if (!open || cur.count + len > GROUP_KEYS || cur.nsegs + 1 > GROUP_MAX_SEGS ||
+        cur.start + cur.count != b) {
+      close(s);
+      cur = SegGroup{b, 0, uint32_t(L.rel.size()), 0, 0};
+      cur_max = 0;
+      cur_first = s;
+      open = true;
+    }
+    L.rel.push_back(cur.count);
+    cur.count += uint32_t(len);
+    cur.nsegs += 1;
+    cur_max = std::max(cur_max, uint32_t(len));
+  }
+  close(nseg);
+  if (L.tiles > 0xFFFFFFF0ull) return "too many tiles";
+  L.tile_start.push_back(uint32_t(L.tiles));
+  return "";
+}
+
+std::string seg_layout_summary(const uint64_t* off, uint32_t nseg, uint64_t n, uint32_t tile,
+                               uint8_t* kinds, uint64_t counts[4]) {
+  SegLayout L;
+  const std::string err = seg_layout(off, nseg, n, tile, L, kinds);
+  if (err.empty()) {
+    counts[0] = L.groups.size();
+    counts[1] = L.tiny.size();
+    counts[2] = L.range.size() / 2;
+    counts[3] = L.tiles;
+  }
+  return err;
+}
+
 // Build a plan from host offsets (nseg + 1 entries). Returns an error text
 // or empty on success.
 std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, uint64_t n,
@@ -447,80 +542,24 @@ std::string seg_plan_build(gs_seg_plan* pl, const uint64_t* off, uint32_t nseg, 
   pl->n = n;
   pl->shape = shape;
   pl->tile = radix_shape_tile(key_bytes, 0, shape);
-  if (off[0] != 0 || off[nseg] != n) return "offsets must start at 0 and end at n";
-  std::vector<SegGroup> groups;
-  std::vector<TinySeg> tiny;
-  std::vector<uint32_t> rel;
-  std::vector<uint32_t> tile_start;
-  std::vector<SegTile> tile_desc;
-  std::vector<uint64_t> range;
-  SegGroup cur{};
-  uint32_t cur_max = 0;  // longest segment of the open group
-  bool open = false;
-  auto close = [&]() {
-    if (open && cur.count > 0 && cur_max <= TINY_KEYS) {
-      // Only tiny segments: one warp each instead of a group sort.
-      rel.push_back(cur.count);
-      for (uint32_t i = 0; i < cur.nsegs; ++i) {
-        const uint32_t a = rel[cur.first_seg + i], z = rel[cur.first_seg + i + 1];
-        tiny.push_back(TinySeg{cur.start + a, z - a, 0});
-      }
-      rel.resize(cur.first_seg);
-    } else if (open && cur.count > 0) {
-      rel.push_back(cur.count);  // end of the last segment
-      groups.push_back(cur);
-    } else if (open) {
-      rel.resize(cur.first_seg);  // empty group: drop its starts
-    }
-    open = false;
-  };
-  uint64_t tiles = 0;
-  for (uint32_t s = 0; s < nseg; ++s) {
-    const uint64_t b = off[s], e = off[s + 1];
-    if (e < b) return "offsets must be non-decreasing";
-    const uint64_t len = e - b;
-    if (len == 0) continue;  // nothing to move
-    if (len > GROUP_KEYS) {
-      close();
-      tile_start.push_back(uint32_t(tiles));
-      const uint32_t large_index = uint32_t(range.size() / 2);
-      range.push_back(b);
-      range.push_back(e);
-      for (uint64_t x = b; x < e; x += pl->tile)
-        tile_desc.push_back(SegTile{x, uint32_t(std::min<uint64_t>(pl->tile, e - x)), large_index});
-      tiles += (len + pl->tile - 1) / pl->tile;
-      continue;
-    }
-    if (!open || cur.count + len > GROUP_KEYS || cur.nsegs + 1 > GROUP_MAX_SEGS ||
-        cur.start + cur.count != b) {
-      close();
-      cur = SegGroup{b, 0, uint32_t(rel.size()), 0, 0};
-      cur_max = 0;
-      open = true;
-    }
-    rel.push_back(cur.count);
-    cur.count += uint32_t(len);
-    cur.nsegs += 1;
-    cur_max = std::max(cur_max, uint32_t(len));
-  }
-  close();
-  if (tiles > 0xFFFFFFF0ull) return "too many tiles";
-  tile_start.push_back(uint32_t(tiles));
-  pl->ngroups = uint32_t(groups.size());
-  pl->ntiny = uint32_t(tiny.size());
-  pl->nlarge = uint32_t(range.size() / 2);
-  pl->large_tiles = uint32_t(tiles);
+  SegLayout L;
+  const std::string err = seg_layout(off, nseg, n, pl->tile, L, nullptr);
+  if (!err.empty()) return err;
+  pl->ngroups = uint32_t(L.groups.size());
+  pl->ntiny = uint32_t(L.tiny.size());
+  pl->nlarge = uint32_t(L.range.size() / 2);
+  pl->large_tiles = uint32_t(L.tiles);
   auto up = [](void** dst, const void* src, size_t bytes) -> bool {
     if (bytes == 0) return true;
     if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
   };
-  bool ok = up(reinterpret_cast<void**>(&pl->d_groups), groups.data(), groups.size() * sizeof(SegGroup)) &&
-            up(reinterpret_cast<void**>(&pl->d_tiny), tiny.data(), tiny.size() * sizeof(TinySeg)) &&
-            up(reinterpret_cast<void**>(&pl->d_starts_rel), rel.data(), rel.size() * 4) &&
-            up(reinterpret_cast<void**>(&pl->d_tile_start), tile_start.data(), tile_start.size() * 4) &&
-            up(reinterpret_cast<void**>(&pl->d_tiles), tile_desc.data(), tile_desc.size() * sizeof(SegTile)) &&
-            up(reinterpret_cast<void**>(&pl->d_range), range.data(), range.size() * 8);
+  bool ok = up(reinterpret_cast<void**>(&pl->d_groups), L.groups.data(), L.groups.size() * sizeof(SegGroup)) &&
+            up(reinterpret_cast<void**>(&pl->d_tiny), L.tiny.data(), L.tiny.size() * sizeof(TinySeg)) &&
+            up(reinterpret_cast<void**>(&pl->d_starts_rel), L.rel.data(), L.rel.size() * 4) &&
+            up(reinterpret_cast<void**>(&pl->d_tile_start), L.tile_start.data(), L.tile_start.size() * 4) &&
+            up(reinterpret_cast<void**>(&pl->d_tiles), L.tile_desc.data(), L.tile_desc.size() * sizeof(SegTile)) &&
+            up(reinterpret_cast<void**>(&pl->d_range), L.range.data(), L.range.size() * 8);
   if (ok && pl->nlarge) {
     ok = cudaMalloc(&pl->d_hist, size_t(pl->nlarge) * key_bytes * RADIX * 4) == cudaSuccess &&
          cudaMalloc(&pl->d_work, sizeof(SortWork)) == cudaSuccess;

@@ -178,6 +178,26 @@ gs_status gs_segmented_plan_run(gs_ctx* ctx, const gs_seg_plan* plan,
                                 const void* in, void* out);
 void gs_segmented_plan_destroy(gs_seg_plan* plan);
 
+/* How a segmented sort of these host offsets treats each segment, computed
+ * on the host alone (no context, no device): `kinds` (nseg entries, may be
+ * null) receives a gs_seg_kind per segment; counts[0..3] receive the
+ * number of groups sorted whole in shared memory, of segments sorted by
+ * one warp each, of segments sorted by the radix passes, and of pass tiles
+ * over those. The rules: segments of at most 4096 keys are packed in order
+ * into groups of consecutive segments (at most 4096 keys and 256 segments
+ * per group); a group made only of segments of at most 32 keys becomes one
+ * warp per segment; longer segments take the passes, in tiles of the pass
+ * shape a plan chooses by default. Same offsets contract as
+ * gs_segmented_plan_create. */
+typedef enum gs_seg_kind {
+  GS_SEG_EMPTY = 0,
+  GS_SEG_WARP = 1,
+  GS_SEG_GROUP = 2,
+  GS_SEG_PASSES = 3
+} gs_seg_kind;
+gs_status gs_segmented_layout(gs_dtype dtype, uint64_t n, const uint64_t* host_offsets,
+                              uint32_t nseg, uint8_t* kinds, uint64_t counts[4]);
+
 /* Apply a permutation to a value array: out[i] = in[perm[i]], element size
  * `elem_bytes` (1..64 bytes). Replaces ParUtils::ArrangeValues
  * (include/par/par_utils.h:23-86), which moves each value vector to where
